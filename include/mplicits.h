@@ -1,0 +1,170 @@
+/*
+ * mplicits.h -- C ABI of libmplicits.so, the GB300 (sm_103a) kernels for the
+ * M-plicits nested sine-MLP hot path: f = f0 + f1 + f2, each residual level
+ * evaluated only inside the delta-band of the previous partial sum, band-culled
+ * marching cubes, sphere tracing and analytic normals.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (MPL_OK == 0); nothing throws.
+ *  - All pointers named *_dev, and every array argument unless stated
+ *    otherwise, are device pointers owned by the caller.  The library never
+ *    allocates device memory inside a call: scratch space is caller-provided
+ *    and sized by the matching *_bytes query.
+ *  - `stream` is a cudaStream_t passed as void*; every launch is
+ *    stream-ordered, and no call synchronises the host unless its comment
+ *    says so.
+ *  - A SIREN level is the network of i3d/model.py:76-103: n_layers nn.Linear
+ *    layers, dims[l] -> dims[l+1], each but the last followed by
+ *    sin(omega[l] * .).  Weights are the nn.Linear tensors, [out, in]
+ *    row-major float32.
+ */
+#ifndef MPLICITS_H_
+#define MPLICITS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPL_ABI_VERSION 1
+#define MPL_MAX_LAYERS 8
+
+/* status codes */
+enum {
+  MPL_OK = 0,
+  MPL_ERR_INVALID_ARG = 1,   /* null pointer, bad size, misaligned buffer     */
+  MPL_ERR_UNSUPPORTED = 2,   /* shape or mode this build has no kernel for    */
+  MPL_ERR_CAPACITY = 3,      /* an output list or workspace is too small      */
+  MPL_ERR_DEVICE_TIMEOUT = 4,/* a bounded device-side wait gave up            */
+  MPL_ERR_CUDA = 5,          /* a CUDA runtime call failed (see last error)   */
+  MPL_ERR_NO_DEVICE = 6      /* no sm_103 device is current                   */
+};
+
+/* arithmetic of the hidden-layer GEMMs */
+enum {
+  MPL_FP32 = 0, /* plain form: FP32 SIMT FMAs, accurate sinf               */
+  MPL_BF16 = 1  /* tcgen05 BF16 MMAs, FP32 accumulate in TMEM, FP32 layer 0 */
+};
+
+/* how a level's output is stored */
+enum {
+  MPL_STORE = 0,     /* S[p]  = f(x_p)                                      */
+  MPL_ACCUMULATE = 1 /* S[p] += f(x_p)   (i3d/meshing.py:231 sdf_base[idx] +=) */
+};
+
+/* where the points come from */
+enum {
+  MPL_POINTS_XYZ = 0, /* explicit float32 [n, 3] coordinates               */
+  MPL_POINTS_GRID = 1 /* grid point p of gen_mc_coordinate_grid, generated
+                         in-kernel with the reference's float32 formula     */
+};
+
+/* Topology of one level. */
+typedef struct MplNet {
+  int32_t n_layers;                  /* nn.Linear layers, 2..MPL_MAX_LAYERS   */
+  int32_t dims[MPL_MAX_LAYERS + 1];  /* dims[0] == 3, dims[n_layers] == 1,
+                                        hidden widths <= 256                   */
+  float omega[MPL_MAX_LAYERS];       /* sine frequency after layer l          */
+} MplNet;
+
+/* A point set.  For MPL_POINTS_GRID point p (0 <= p < N^3) is row p of
+ * gen_mc_coordinate_grid(N, voxel_size) (i3d/meshing.py:42-63), including
+ * the float32 true-division shear of its x and y columns.  offset[c] is the
+ * constant added to column c (the reference adds voxel_origin[2], [1], [0]).*/
+typedef struct MplPoints {
+  int32_t kind;        /* MPL_POINTS_XYZ or MPL_POINTS_GRID                 */
+  int32_t grid_n;      /* N (GRID)                                          */
+  float voxel_size;    /* float32 voxel size (GRID)                          */
+  float offset[3];     /* per-column offset (GRID)                           */
+  const float* xyz;    /* [n, 3] float32 (XYZ)                               */
+} MplPoints;
+
+/* Fused band compaction: after a level stores S[p], p is appended to
+ * out_index when |S[p]| < delta (float32 compare, i3d/meshing.py:223).
+ * *count_dev is reset to 0 by the call.  Entries past `capacity` are dropped
+ * but still counted, so *count_dev > capacity reports an overflow.  The
+ * order of out_index is unspecified; its set is exact. */
+typedef struct MplBand {
+  float delta;
+  int32_t* out_index;  /* device [capacity]                                  */
+  int32_t* count_dev;  /* device int32 scalar                                */
+  int64_t capacity;
+} MplBand;
+
+/* ---- weights ------------------------------------------------------------ */
+
+/* Bytes of the packed device image of one level (FP32 and BF16 forms). */
+int mpl_net_packed_bytes(const MplNet* net, int64_t* bytes);
+
+/* Packs a level's nn.Linear tensors (device pointers, weights[l] is
+ * [dims[l+1], dims[l]], biases[l] is [dims[l+1]]) into `packed_dev`
+ * (>= mpl_net_packed_bytes, 256-byte aligned).  Replaces the per-layer
+ * tensors the reference's LayerGemm holds (renderer/cuda/gemms.cu:5-100). */
+int mpl_net_pack(const MplNet* net, const float* const* weights_dev,
+                 const float* const* biases_dev, void* packed_dev, void* stream);
+
+/* ---- level evaluation (i3d/model.py:107-129; i3d/meshing.py:212-236) ---- */
+
+/* Evaluates one level on points q = 0..n-1, where the point is
+ * p = index ? index[q] : q, and stores or accumulates f(x_p) into S[p].
+ * If n_dev is non-null, the point count is min(*n_dev, n) read on the
+ * device (so a band list produced by a previous call can be consumed
+ * without a host round trip).  `band` (nullable) appends the points of
+ * the next delta-band.  precision: MPL_FP32 or MPL_BF16. */
+int mpl_level_forward(const MplNet* net, const void* packed_dev, const MplPoints* points,
+                      const int32_t* index_dev, const int32_t* n_dev, int64_t n,
+                      float* S_dev, int32_t store_mode, const MplBand* band,
+                      int32_t precision, void* stream);
+
+/* Writes the float32 coordinates [n, 3] of grid points p = index ? index[q]
+ * : q (points->kind must be MPL_POINTS_GRID): the columns 0..2 of
+ * gen_mc_coordinate_grid (i3d/meshing.py:11-69), bit for bit. */
+int mpl_grid_points(const MplPoints* points, const int32_t* index_dev, int64_t n,
+                    float* xyz_dev, void* stream);
+
+/* ---- band compaction (i3d/meshing.py:222-231) --------------------------- */
+
+/* Appends q's point p = index ? index[q] : q for q < n (or < *n_dev) with
+ * |S[p]| < band->delta to band->out_index. */
+int mpl_band_compact(const float* S_dev, const int32_t* index_dev, const int32_t* n_dev,
+                     int64_t n, const MplBand* band, void* stream);
+
+/* ---- marching cubes (i3d/meshing.py:267-313; scikit-image's
+ *      marching_cubes, replaced by a table derived in this project) ------- */
+
+/* Workspace bytes for an N^3 volume. */
+int mpl_mc_workspace_bytes(int64_t N, int64_t* bytes);
+
+/* Classifies every cell of the C-order N^3 volume S and writes
+ * counts_dev[0] = vertices, counts_dev[1] = triangles (int64). */
+int mpl_mc_count(const float* S_dev, int64_t N, float iso, void* workspace_dev,
+                 int64_t* counts_dev, void* stream);
+
+/* Emits the mesh counted by the preceding mpl_mc_count on the same
+ * workspace.  Vertices are ordered by (lower grid point, axis) of their edge,
+ * faces by cell then case-table order.  verts/normals [V,3] f32, values [V]
+ * f32 (nullable), faces [F,3] int32.  Coordinates are
+ * ((float)index + t) * voxel_size + origin[axis]. */
+int mpl_mc_emit(const float* S_dev, int64_t N, float iso, float voxel_size,
+                const float* origin_host, const void* workspace_dev, float* verts_dev,
+                float* normals_dev, float* values_dev, int32_t* faces_dev, int64_t max_verts,
+                int64_t max_tris, void* stream);
+
+/* ---- diagnostics -------------------------------------------------------- */
+
+const char* mpl_status_string(int status);
+/* Synchronises the device, then reads and clears the device status word that
+ * bounded device-side waits set when they give up (MPL_ERR_DEVICE_TIMEOUT);
+ * *status_out is MPL_OK when no wait gave up. */
+int mpl_device_status(int32_t* status_out);
+/* cudaError_t of the most recent failed CUDA call in this thread. */
+int mpl_last_cuda_error(void);
+int mpl_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPLICITS_H_ */

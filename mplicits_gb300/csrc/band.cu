@@ -1,0 +1,60 @@
+// Band compaction, i3d/meshing.py:222-231 (`idx = |sdf_base| < delta`
+// followed by the boolean gather `sample_subset[idx]`): a warp-ballot
+// stream compaction of the points of a delta-band into an index list.
+// HBM-bound: 4 B read per candidate, 4 B written per kept point.
+#include "level.cuh"
+
+namespace mpl {
+
+__global__ void band_compact_kernel(const float* __restrict__ S, const int32_t* __restrict__ index,
+                                    const int32_t* __restrict__ n_dev, int64_t n, float delta,
+                                    int32_t* __restrict__ out, int32_t* __restrict__ count,
+                                    int64_t capacity) {
+  if (n_dev) {
+    const int64_t m = *n_dev;
+    n = m < n ? m : n;
+  }
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // every lane of a warp runs the same number of iterations (ballot safety)
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) - lane;
+  for (int64_t base = warp0; base < n; base += stride) {
+    const int64_t q = base + lane;
+    bool keep = false;
+    int64_t p = 0;
+    if (q < n) {
+      p = index ? (int64_t)index[q] : q;
+      keep = fabsf(S[p]) < delta;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int b = 0;
+    if (lane == 0 && m) b = atomicAdd(count, __popc(m));
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (keep) {
+      const int64_t pos = (int64_t)b + __popc(m & ((1u << lane) - 1u));
+      if (pos < capacity) out[pos] = (int32_t)p;
+    }
+  }
+}
+
+}  // namespace mpl
+
+using namespace mpl;
+
+extern "C" int mpl_band_compact(const float* S, const int32_t* index, const int32_t* n_dev,
+                                int64_t n, const MplBand* band, void* stream) {
+  if (!S || !band || !band->out_index || !band->count_dev || n < 0 || n > INT32_MAX)
+    return MPL_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  MPL_CUDA_TRY(cudaMemsetAsync(band->count_dev, 0, sizeof(int32_t), s));
+  if (n == 0) return MPL_OK;
+  const int threads = 256;
+  int64_t blocks = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)sm_count() * 8;
+  if (blocks > cap) blocks = cap;
+  band_compact_kernel<<<(unsigned)blocks, threads, 0, s>>>(S, index, n_dev, n, band->delta,
+                                                           band->out_index, band->count_dev,
+                                                           band->capacity);
+  MPL_LAUNCH_CHECK();
+  return MPL_OK;
+}

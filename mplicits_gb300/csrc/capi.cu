@@ -1,0 +1,114 @@
+// extern "C" entry points of libmplicits: argument validation and dispatch.
+#include <string.h>
+
+#include "level.cuh"
+
+namespace mpl {
+
+__device__ int g_device_status = 0;
+
+int* device_status_ptr() {
+  static int* cached[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!cached[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_device_status) != cudaSuccess) return nullptr;
+    cached[dev] = (int*)p;
+  }
+  return cached[dev];
+}
+
+static thread_local int t_last_cuda_error = 0;
+
+void set_last_cuda_error(cudaError_t e) { t_last_cuda_error = (int)e; }
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cached[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 148;
+  }
+  return cached[dev];
+}
+
+}  // namespace mpl
+
+using namespace mpl;
+
+extern "C" int mpl_level_forward(const MplNet* net, const void* packed, const MplPoints* points,
+                                 const int32_t* index, const int32_t* n_dev, int64_t n,
+                                 float* S, int32_t store_mode, const MplBand* band,
+                                 int32_t precision, void* stream) {
+  if (!net || !packed || !points || !S || n < 0 || n > INT32_MAX) return MPL_ERR_INVALID_ARG;
+  if (((uintptr_t)packed & 255) != 0) return MPL_ERR_INVALID_ARG;
+  if (store_mode != MPL_STORE && store_mode != MPL_ACCUMULATE) return MPL_ERR_INVALID_ARG;
+  if (points->kind == MPL_POINTS_XYZ) {
+    if (!points->xyz) return MPL_ERR_INVALID_ARG;
+  } else if (points->kind == MPL_POINTS_GRID) {
+    if (points->grid_n < 2) return MPL_ERR_INVALID_ARG;
+    const int64_t N = points->grid_n;
+    if (N * N * N > (int64_t)INT32_MAX + 1) return MPL_ERR_UNSUPPORTED;
+  } else {
+    return MPL_ERR_INVALID_ARG;
+  }
+  LevelArgs a;
+  memset(&a, 0, sizeof(a));
+  int st = make_layout(net, &a.lay);
+  if (st != MPL_OK) return st;
+  a.packed = (const char*)packed;
+  for (int l = 0; l < MPL_MAX_LAYERS; ++l) a.omega[l] = net->omega[l];
+  a.pts = *points;
+  a.index = index;
+  a.n_dev = n_dev;
+  a.n = n;
+  a.S = S;
+  a.store_mode = store_mode;
+  a.status = device_status_ptr();
+  cudaStream_t s = (cudaStream_t)stream;
+  if (band) {
+    if (!band->out_index || !band->count_dev || band->capacity < 0) return MPL_ERR_INVALID_ARG;
+    a.has_band = 1;
+    a.band_delta = band->delta;
+    a.band_out = band->out_index;
+    a.band_count = band->count_dev;
+    a.band_capacity = band->capacity;
+    MPL_CUDA_TRY(cudaMemsetAsync(band->count_dev, 0, sizeof(int32_t), s));
+  }
+  if (n == 0) return MPL_OK;
+  if (precision == MPL_FP32) return launch_level_fp32(a, s);
+  if (precision == MPL_BF16) return launch_level_bf16(a, s);
+  return MPL_ERR_INVALID_ARG;
+}
+
+extern "C" const char* mpl_status_string(int status) {
+  switch (status) {
+    case MPL_OK: return "ok";
+    case MPL_ERR_INVALID_ARG: return "invalid argument";
+    case MPL_ERR_UNSUPPORTED: return "unsupported shape or mode";
+    case MPL_ERR_CAPACITY: return "output capacity exceeded";
+    case MPL_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case MPL_ERR_CUDA: return "CUDA runtime error";
+    case MPL_ERR_NO_DEVICE: return "no suitable CUDA device";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int mpl_last_cuda_error(void) { return t_last_cuda_error; }
+
+extern "C" int mpl_abi_version(void) { return MPL_ABI_VERSION; }
+
+// Reads and clears the device status word (synchronises the device).
+extern "C" int mpl_device_status(int32_t* status_out) {
+  if (!status_out) return MPL_ERR_INVALID_ARG;
+  int v = 0;
+  MPL_CUDA_TRY(cudaDeviceSynchronize());
+  MPL_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_device_status, sizeof(int)));
+  const int zero = 0;
+  MPL_CUDA_TRY(cudaMemcpyToSymbol(g_device_status, &zero, sizeof(int)));
+  *status_out = v;
+  return MPL_OK;
+}

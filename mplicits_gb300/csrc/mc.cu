@@ -1,0 +1,394 @@
+// Marching cubes on the GPU, replacing the CPU call to scikit-image's
+// marching_cubes in convert_sdf_samples_to_ply (i3d/meshing.py:291-313)
+// and the 512 MiB device->host copy before it (i3d/meshing.py:242).
+//
+// The volume is C-order [N][N][N]; a *row* is the N points (i, j, 0..N-1).
+//   count:  one warp per row classifies its points (crossing edges owned by
+//           each point) and cells (case -> triangle count) and writes the
+//           row totals;
+//   scan:   exclusive prefix sums of the row totals (int64);
+//   emit:   one CTA per non-empty row rebuilds the in-row vertex prefixes of
+//           the four rows a cell touches with warp scans, writes the row's
+//           vertices and its triangles.
+// Output order is canonical (see mplicits.h) and matches the CPU restatement
+// in oracle/mc.c bit for bit: all arithmetic is float32 with explicit
+// round-to-nearest intrinsics and no contraction.
+#include "common.cuh"
+#include "mc_tables.h"
+
+namespace mpl {
+
+namespace {
+
+__constant__ unsigned char c_tri_count[256];
+__constant__ signed char c_tri_edges[256][MPL_MC_MAX_TRIS * 3];
+__constant__ signed char c_edge[12][7];
+
+struct McWork {
+  int32_t* row_v;   // [N*N]
+  int32_t* row_t;   // [N*N]
+  int64_t* pre_v;   // [N*N]
+  int64_t* pre_t;   // [N*N]
+  int64_t* blk;     // [2 * nblk]
+  int64_t* totals;  // [2]
+};
+
+constexpr int kScanChunk = 2048;  // rows per scan block
+
+__host__ __device__ inline int64_t mc_nblk(int64_t N) {
+  return (N * N + kScanChunk - 1) / kScanChunk;
+}
+
+__host__ __device__ inline McWork mc_work(void* base, int64_t N) {
+  McWork w;
+  char* p = (char*)base;
+  const int64_t R = N * N;
+  w.row_v = (int32_t*)p;
+  p += align256(R * 4);
+  w.row_t = (int32_t*)p;
+  p += align256(R * 4);
+  w.pre_v = (int64_t*)p;
+  p += align256(R * 8);
+  w.pre_t = (int64_t*)p;
+  p += align256(R * 8);
+  w.blk = (int64_t*)p;
+  p += align256(2 * mc_nblk(N) * 8);
+  w.totals = (int64_t*)p;
+  return w;
+}
+
+__host__ inline int64_t mc_work_bytes(int64_t N) {
+  const int64_t R = N * N;
+  return align256(R * 4) * 2 + align256(R * 8) * 2 + align256(2 * mc_nblk(N) * 8) + 256;
+}
+
+__device__ __forceinline__ int point_mask(const float* __restrict__ S, int64_t N, int64_t i,
+                                          int64_t j, int64_t k, float iso) {
+  const int64_t p = (i * N + j) * N + k;
+  const bool s = S[p] < iso;
+  int m = 0;
+  if (i + 1 < N && ((S[p + N * N] < iso) != s)) m |= 1;
+  if (j + 1 < N && ((S[p + N] < iso) != s)) m |= 2;
+  if (k + 1 < N && ((S[p + 1] < iso) != s)) m |= 4;
+  return m;
+}
+
+__device__ __forceinline__ int cell_case(const float* __restrict__ S, int64_t N, int64_t i,
+                                         int64_t j, int64_t k, float iso) {
+  int c = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int64_t p = ((i + (q & 1)) * N + (j + ((q >> 1) & 1))) * N + (k + ((q >> 2) & 1));
+    c |= (S[p] < iso ? 1 : 0) << q;
+  }
+  return c;
+}
+
+__global__ void mc_count_kernel(const float* __restrict__ S, int64_t N, float iso, McWork w) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (r >= N * N) return;
+  const int64_t i = r / N, j = r % N;
+  const bool cells = (i + 1 < N) && (j + 1 < N);
+  int nv = 0, nt = 0;
+  for (int64_t k = lane; k < N; k += 32) {
+    nv += __popc(point_mask(S, N, i, j, k, iso));
+    if (cells && k + 1 < N) nt += c_tri_count[cell_case(S, N, i, j, k, iso)];
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    nv += __shfl_xor_sync(0xffffffffu, nv, o);
+    nt += __shfl_xor_sync(0xffffffffu, nt, o);
+  }
+  if (lane == 0) {
+    w.row_v[r] = nv;
+    w.row_t[r] = nt;
+  }
+}
+
+// block-wide exclusive scan of one int64 per thread (blockDim.x a multiple
+// of 32, at most 256)
+__device__ int64_t block_exclusive_scan(int64_t v, int64_t* total) {
+  __shared__ int64_t warp_sums[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int64_t s = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const int64_t before = wid > 0 ? warp_sums[wid - 1] : 0;
+  if (total) *total = warp_sums[nw - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// phase 1: per-block exclusive scan of kScanChunk rows (256 threads x 8)
+__global__ void mc_scan_blocks(int64_t N, McWork w) {
+  const int64_t R = N * N;
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk + threadIdx.x * 8;
+  int64_t lv[8], lt[8], sv = 0, st = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int64_t r = base + q;
+    lv[q] = r < R ? w.row_v[r] : 0;
+    lt[q] = r < R ? w.row_t[r] : 0;
+    sv += lv[q];
+    st += lt[q];
+  }
+  int64_t tv, tt;
+  int64_t ov = block_exclusive_scan(sv, &tv);
+  int64_t ot = block_exclusive_scan(st, &tt);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int64_t r = base + q;
+    if (r < R) {
+      w.pre_v[r] = ov;
+      w.pre_t[r] = ot;
+    }
+    ov += lv[q];
+    ot += lt[q];
+  }
+  if (threadIdx.x == 0) {
+    w.blk[2 * blockIdx.x] = tv;
+    w.blk[2 * blockIdx.x + 1] = tt;
+  }
+}
+
+// phase 2: one CTA scans the block totals in place, writes the grand totals
+__global__ void mc_scan_top(int64_t nblk, McWork w, int64_t* counts_out) {
+  int64_t carry_v = 0, carry_t = 0;
+  for (int64_t b0 = 0; b0 < nblk; b0 += blockDim.x) {
+    const int64_t b = b0 + threadIdx.x;
+    const int64_t v = b < nblk ? w.blk[2 * b] : 0;
+    const int64_t t = b < nblk ? w.blk[2 * b + 1] : 0;
+    int64_t tv, tt;
+    const int64_t ev = block_exclusive_scan(v, &tv);
+    const int64_t et = block_exclusive_scan(t, &tt);
+    if (b < nblk) {
+      w.blk[2 * b] = carry_v + ev;
+      w.blk[2 * b + 1] = carry_t + et;
+    }
+    carry_v += tv;
+    carry_t += tt;
+  }
+  if (threadIdx.x == 0) {
+    w.totals[0] = carry_v;
+    w.totals[1] = carry_t;
+    if (counts_out) {
+      counts_out[0] = carry_v;
+      counts_out[1] = carry_t;
+    }
+  }
+}
+
+// phase 3: add block offsets
+__global__ void mc_scan_add(int64_t N, McWork w) {
+  const int64_t R = N * N;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const int64_t b = r / kScanChunk;
+  w.pre_v[r] += w.blk[2 * b];
+  w.pre_t[r] += w.blk[2 * b + 1];
+}
+
+__device__ __forceinline__ float grad_axis(const float* __restrict__ S, int64_t N,
+                                           const int64_t idx[3], int axis) {
+  int64_t lo[3] = {idx[0], idx[1], idx[2]};
+  int64_t hi[3] = {idx[0], idx[1], idx[2]};
+  if (idx[axis] > 0) lo[axis] -= 1;
+  if (idx[axis] + 1 < N) hi[axis] += 1;
+  const float d = __fsub_rn(S[(hi[0] * N + hi[1]) * N + hi[2]], S[(lo[0] * N + lo[1]) * N + lo[2]]);
+  return __fdiv_rn(d, (float)(hi[axis] - lo[axis]));
+}
+
+constexpr int kEmitThreads = 128;
+constexpr int kMaxN = 1024;
+
+// one CTA (4 warps) per row r = (i, j)
+__global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(
+    const float* __restrict__ S, int64_t N, float iso, float vs, float o0, float o1, float o2,
+    McWork w, float* __restrict__ verts, float* __restrict__ normals, float* __restrict__ values,
+    int32_t* __restrict__ faces, int64_t max_verts, int64_t max_tris) {
+  __shared__ int32_t pre[4][kMaxN];
+  __shared__ uint8_t msk[4][kMaxN];
+  const int64_t r = blockIdx.x;
+  const int64_t i = r / N, j = r % N;
+  if (w.row_v[r] == 0 && w.row_t[r] == 0) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const float org[3] = {o0, o1, o2};
+
+  // rows touched by the cells of row (i, j): 0:(i,j) 1:(i,j+1) 2:(i+1,j) 3:(i+1,j+1)
+  {
+    const int64_t ri = i + (wid >> 1), rj = j + (wid & 1);
+    if (ri < N && rj < N) {
+      int32_t carry = 0;
+      for (int64_t k0 = 0; k0 < N; k0 += 32) {
+        const int64_t k = k0 + lane;
+        const int m = k < N ? point_mask(S, N, ri, rj, k, iso) : 0;
+        int x = __popc(m);
+        const int own = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        if (k < N) {
+          pre[wid][k] = carry + x - own;
+          msk[wid][k] = (uint8_t)m;
+        }
+        carry += __shfl_sync(0xffffffffu, x, 31);
+      }
+    }
+  }
+  __syncthreads();
+
+  // vertices of row (i, j)
+  const int64_t vbase = w.pre_v[r];
+  for (int64_t k = threadIdx.x; k < N; k += kEmitThreads) {
+    const int m = msk[0][k];
+    if (!m) continue;
+    int64_t v = vbase + pre[0][k];
+    const int64_t p = (i * N + j) * N + k;
+    for (int a = 0; a < 3; ++a) {
+      if (!(m & (1 << a))) continue;
+      if (v < max_verts) {
+        const int64_t idx0[3] = {i, j, k};
+        int64_t idx1[3] = {i, j, k};
+        idx1[a] += 1;
+        const float v0 = S[p];
+        const float v1 = S[(idx1[0] * N + idx1[1]) * N + idx1[2]];
+        const float t = __fdiv_rn(__fsub_rn(iso, v0), __fsub_rn(v1, v0));
+        float n[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          float c = (float)idx0[d];
+          if (d == a) c = __fadd_rn(c, t);
+          verts[3 * v + d] = __fadd_rn(__fmul_rn(c, vs), org[d]);
+          const float g0 = grad_axis(S, N, idx0, d);
+          const float g1 = grad_axis(S, N, idx1, d);
+          n[d] = __fadd_rn(g0, __fmul_rn(t, __fsub_rn(g1, g0)));
+        }
+        float l2 = __fmul_rn(n[0], n[0]);
+        l2 = __fadd_rn(l2, __fmul_rn(n[1], n[1]));
+        l2 = __fadd_rn(l2, __fmul_rn(n[2], n[2]));
+        const float len = __fsqrt_rn(l2);
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          normals[3 * v + d] = len > 0.0f ? __fdiv_rn(n[d], len) : 0.0f;
+        if (values) values[v] = v0 > v1 ? v0 : v1;
+      }
+      ++v;
+    }
+  }
+
+  // triangles of the cells of row (i, j)
+  if (i + 1 >= N || j + 1 >= N) return;
+  int64_t tcarry = w.pre_t[r];
+  for (int64_t k0 = 0; k0 < N - 1; k0 += kEmitThreads) {
+    const int64_t k = k0 + threadIdx.x;
+    int c = 0, nt = 0;
+    if (k < N - 1) {
+      c = cell_case(S, N, i, j, k, iso);
+      nt = c_tri_count[c];
+    }
+    int64_t tot;
+    const int64_t off = block_exclusive_scan(nt, &tot);
+    int64_t t = tcarry + off;
+    for (int q = 0; q < nt; ++q, ++t) {
+      if (t >= max_tris) break;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int e = c_tri_edges[c][3 * q + s];
+        const int axis = c_edge[e][0];
+        const int row = c_edge[e][1] * 2 + c_edge[e][2];
+        const int64_t kk = k + c_edge[e][3];
+        const int64_t rr = (i + c_edge[e][1]) * N + (j + c_edge[e][2]);
+        const int64_t vid = w.pre_v[rr] + pre[row][kk] +
+                            __popc((int)msk[row][kk] & ((1 << axis) - 1));
+        faces[3 * t + s] = (int32_t)vid;
+      }
+    }
+    tcarry += tot;
+  }
+}
+
+bool g_tables_loaded[64] = {false};
+
+int ensure_tables() {
+  int dev = 0;
+  MPL_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return MPL_ERR_INVALID_ARG;
+  if (g_tables_loaded[dev]) return MPL_OK;
+  MPL_CUDA_TRY(cudaMemcpyToSymbol(c_tri_count, MPL_MC_TRI_COUNT, sizeof(MPL_MC_TRI_COUNT)));
+  MPL_CUDA_TRY(cudaMemcpyToSymbol(c_tri_edges, MPL_MC_TRI_EDGES, sizeof(MPL_MC_TRI_EDGES)));
+  MPL_CUDA_TRY(cudaMemcpyToSymbol(c_edge, MPL_MC_EDGE, sizeof(MPL_MC_EDGE)));
+  g_tables_loaded[dev] = true;
+  return MPL_OK;
+}
+
+}  // namespace
+
+}  // namespace mpl
+
+using namespace mpl;
+
+extern "C" int mpl_mc_workspace_bytes(int64_t N, int64_t* bytes) {
+  if (!bytes || N < 2 || N > kMaxN) return N > kMaxN ? MPL_ERR_UNSUPPORTED : MPL_ERR_INVALID_ARG;
+  *bytes = mc_work_bytes(N);
+  return MPL_OK;
+}
+
+extern "C" int mpl_mc_count(const float* S, int64_t N, float iso, void* workspace,
+                            int64_t* counts_dev, void* stream) {
+  if (!S || !workspace || N < 2) return MPL_ERR_INVALID_ARG;
+  if (N > kMaxN) return MPL_ERR_UNSUPPORTED;
+  if (((uintptr_t)workspace & 255) != 0) return MPL_ERR_INVALID_ARG;
+  int st = ensure_tables();
+  if (st != MPL_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  McWork w = mc_work(workspace, N);
+  const int64_t R = N * N;
+  mc_count_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(S, N, iso, w);
+  MPL_LAUNCH_CHECK();
+  const int64_t nblk = mc_nblk(N);
+  mc_scan_blocks<<<(unsigned)nblk, 256, 0, s>>>(N, w);
+  MPL_LAUNCH_CHECK();
+  mc_scan_top<<<1, 256, 0, s>>>(nblk, w, counts_dev);
+  MPL_LAUNCH_CHECK();
+  mc_scan_add<<<(unsigned)((R + 255) / 256), 256, 0, s>>>(N, w);
+  MPL_LAUNCH_CHECK();
+  return MPL_OK;
+}
+
+extern "C" int mpl_mc_emit(const float* S, int64_t N, float iso, float voxel_size,
+                           const float* origin, const void* workspace, float* verts,
+                           float* normals, float* values, int32_t* faces, int64_t max_verts,
+                           int64_t max_tris, void* stream) {
+  if (!S || !workspace || !origin || N < 2) return MPL_ERR_INVALID_ARG;
+  if (N > kMaxN) return MPL_ERR_UNSUPPORTED;
+  if ((max_verts > 0 && (!verts || !normals)) || (max_tris > 0 && !faces))
+    return MPL_ERR_INVALID_ARG;
+  int st = ensure_tables();
+  if (st != MPL_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  McWork w = mc_work(const_cast<void*>(workspace), N);
+  mc_emit_kernel<<<(unsigned)(N * N), kEmitThreads, 0, s>>>(
+      S, N, iso, voxel_size, origin[0], origin[1], origin[2], w, verts, normals, values, faces,
+      max_verts, max_tris);
+  MPL_LAUNCH_CHECK();
+  return MPL_OK;
+}
