@@ -93,6 +93,18 @@ typedef struct MplBand {
   int64_t capacity;
 } MplBand;
 
+/* A pinhole camera: look-at eye/target/up, vertical field of view, image
+ * size.  Pixel (i, j) has NDC x = 2i/W - 1 and y = 1 - 2j/H, as the
+ * reference's ray tests (renderer/cuda/tests/tests.cu:73-87). */
+typedef struct MplCamera {
+  float eye[3];
+  float target[3];
+  float up[3];
+  float fov_y_deg;
+  int32_t width;
+  int32_t height;
+} MplCamera;
+
 /* ---- weights ------------------------------------------------------------ */
 
 /* Bytes of the packed device image of one level (FP32 and BF16 forms). */
@@ -124,6 +136,17 @@ int mpl_level_forward(const MplNet* net, const void* packed_dev, const MplPoints
 int mpl_grid_points(const MplPoints* points, const int32_t* index_dev, int64_t n,
                     float* xyz_dev, void* stream);
 
+/* As mpl_level_forward, and also stores (or accumulates) the input gradient
+ * df/dx of every point into G[3p .. 3p+2] in one launch, by forward-mode
+ * differentiation through the fused level.  Replaces the autograd gradient
+ * of i3d/diff_operators.py:259-265 (normals, eikonal term) and the
+ * reference renderer's per-coordinate Normals GEMM chains
+ * (renderer/cuda/gemms.cu:206-337, kernels.cu:277-313). */
+int mpl_level_gradient(const MplNet* net, const void* packed_dev, const MplPoints* points,
+                       const int32_t* index_dev, const int32_t* n_dev, int64_t n, float* S_dev,
+                       float* G_dev, int32_t store_mode, const MplBand* band, int32_t precision,
+                       void* stream);
+
 /* ---- band compaction (i3d/meshing.py:222-231) --------------------------- */
 
 /* Appends q's point p = index ? index[q] : q for q < n (or < *n_dev) with
@@ -151,6 +174,37 @@ int mpl_mc_emit(const float* S_dev, int64_t N, float iso, float voxel_size,
                 const float* origin_host, const void* workspace_dev, float* verts_dev,
                 float* normals_dev, float* values_dev, int32_t* faces_dev, int64_t max_verts,
                 int64_t max_tris, void* stream);
+
+/* ---- sphere tracing (renderer/cuda/kernels.cu:315-487, state.cu:848-880) */
+
+/* Generates one ray per pixel into origins/dirs [W*H, 3], moves every origin
+ * outside the bounding sphere of `radius` onto it (kernels.cu:454-477), sets
+ * state[r] = 0 (marching) or 2 (misses the sphere) and writes the marching
+ * rays to active[0 .. *count).  Replaces InitializeRays_kernel
+ * (kernels.cu:400-487). */
+int mpl_trace_init(const MplCamera* camera, float radius, float* origins_dev, float* dirs_dev,
+                   int32_t* state_dev, int32_t* active_dev, int32_t* count_dev, void* stream);
+
+/* One marching step over the rays active[0 .. min(*count, n_max)), whose
+ * distance S[r] the level launches have just produced: |S| < eps marks a hit
+ * (state 1, appended to hit_out / *hit_count, which the caller zeroes once
+ * per frame); otherwise origins += dirs * S, and a ray leaving the sphere
+ * outwards is a miss (state 2); with last_step set the remaining rays get
+ * state 3.  Marching rays go to active_out / *count_out (reset by the call).
+ * Replaces IterateSphereTracing_kernel (kernels.cu:315-398). */
+int mpl_trace_step(const float* S_dev, const int32_t* active_dev, const int32_t* count_dev,
+                   int64_t n_max, float* origins_dev, const float* dirs_dev, int32_t* state_dev,
+                   float eps, float radius, int32_t last_step, int32_t* active_out_dev,
+                   int32_t* count_out_dev, int32_t* hit_out_dev, int32_t* hit_count_dev,
+                   int64_t capacity, void* stream);
+
+/* Shades every pixel into RGBA8 (little-endian R in the low byte): hits
+ * inside [-1,1]^3 with Phong (mode 1) or |normal| colours (mode 0) from the
+ * gradients G [P, 3], everything else white.  Replaces Shade_kernel
+ * (kernels.cu:122-275) writing a headless buffer instead of a GL PBO. */
+int mpl_trace_shade(const float* origins_dev, const float* dirs_dev, const float* G_dev,
+                    const int32_t* state_dev, int64_t P, int32_t mode, uint32_t* image_dev,
+                    void* stream);
 
 /* ---- diagnostics -------------------------------------------------------- */
 

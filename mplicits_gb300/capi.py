@@ -54,6 +54,15 @@ class MplBand(ctypes.Structure):
                 ("capacity", ctypes.c_int64)]
 
 
+class MplCamera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3),
+                ("target", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3),
+                ("fov_y_deg", ctypes.c_float),
+                ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check that the
 # library exports exactly what include/mplicits.h declares.
 _P = ctypes.c_void_p
@@ -66,11 +75,18 @@ SIGNATURES = {
     "mpl_level_forward": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, ctypes.POINTER(MplPoints),
                                          _P, _P, _I64, _P, _I32, ctypes.POINTER(MplBand), _I32,
                                          _P]),
+    "mpl_level_gradient": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, ctypes.POINTER(MplPoints),
+                                          _P, _P, _I64, _P, _P, _I32, ctypes.POINTER(MplBand),
+                                          _I32, _P]),
     "mpl_grid_points": (ctypes.c_int, [ctypes.POINTER(MplPoints), _P, _I64, _P, _P]),
     "mpl_band_compact": (ctypes.c_int, [_P, _P, _P, _I64, ctypes.POINTER(MplBand), _P]),
     "mpl_mc_workspace_bytes": (ctypes.c_int, [_I64, ctypes.POINTER(_I64)]),
     "mpl_mc_count": (ctypes.c_int, [_P, _I64, _F, _P, _P, _P]),
     "mpl_mc_emit": (ctypes.c_int, [_P, _I64, _F, _F, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
+    "mpl_trace_init": (ctypes.c_int, [ctypes.POINTER(MplCamera), _F, _P, _P, _P, _P, _P, _P]),
+    "mpl_trace_step": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _F, _F, _I32, _P, _P, _P, _P,
+                                      _I64, _P]),
+    "mpl_trace_shade": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P]),
     "mpl_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "mpl_device_status": (ctypes.c_int, [ctypes.POINTER(_I32)]),
     "mpl_last_cuda_error": (ctypes.c_int, []),

@@ -39,15 +39,16 @@ int sm_count() {
 
 using namespace mpl;
 
-extern "C" int mpl_level_forward(const MplNet* net, const void* packed, const MplPoints* points,
-                                 const int32_t* index, const int32_t* n_dev, int64_t n,
-                                 float* S, int32_t store_mode, const MplBand* band,
-                                 int32_t precision, void* stream) {
-  if (!net || !packed || !points || !S || n < 0 || n > INT32_MAX) return MPL_ERR_INVALID_ARG;
+static int level_call(const MplNet* net, const void* packed, const MplPoints* points,
+                      const int32_t* index, const int32_t* n_dev, int64_t n, float* S, float* G,
+                      int32_t grad, int32_t store_mode, const MplBand* band, int32_t precision,
+                      void* stream) {
+  if (!net || !packed || !points || n < 0 || n > INT32_MAX) return MPL_ERR_INVALID_ARG;
+  if (!S && (n > 0 || n_dev)) return MPL_ERR_INVALID_ARG;
   if (((uintptr_t)packed & 255) != 0) return MPL_ERR_INVALID_ARG;
   if (store_mode != MPL_STORE && store_mode != MPL_ACCUMULATE) return MPL_ERR_INVALID_ARG;
   if (points->kind == MPL_POINTS_XYZ) {
-    if (!points->xyz) return MPL_ERR_INVALID_ARG;
+    if (!points->xyz && n > 0) return MPL_ERR_INVALID_ARG;
   } else if (points->kind == MPL_POINTS_GRID) {
     if (points->grid_n < 2) return MPL_ERR_INVALID_ARG;
     const int64_t N = points->grid_n;
@@ -68,6 +69,8 @@ extern "C" int mpl_level_forward(const MplNet* net, const void* packed, const Mp
   a.S = S;
   a.store_mode = store_mode;
   a.status = device_status_ptr();
+  a.grad = grad;
+  a.G = G;
   cudaStream_t s = (cudaStream_t)stream;
   if (band) {
     if (!band->out_index || !band->count_dev || band->capacity < 0) return MPL_ERR_INVALID_ARG;
@@ -82,6 +85,24 @@ extern "C" int mpl_level_forward(const MplNet* net, const void* packed, const Mp
   if (precision == MPL_FP32) return launch_level_fp32(a, s);
   if (precision == MPL_BF16) return launch_level_bf16(a, s);
   return MPL_ERR_INVALID_ARG;
+}
+
+extern "C" int mpl_level_forward(const MplNet* net, const void* packed, const MplPoints* points,
+                                 const int32_t* index, const int32_t* n_dev, int64_t n,
+                                 float* S, int32_t store_mode, const MplBand* band,
+                                 int32_t precision, void* stream) {
+  return level_call(net, packed, points, index, n_dev, n, S, nullptr, 0, store_mode, band,
+                    precision, stream);
+}
+
+extern "C" int mpl_level_gradient(const MplNet* net, const void* packed,
+                                  const MplPoints* points, const int32_t* index,
+                                  const int32_t* n_dev, int64_t n, float* S, float* G,
+                                  int32_t store_mode, const MplBand* band, int32_t precision,
+                                  void* stream) {
+  if (!G && (n > 0 || n_dev)) return MPL_ERR_INVALID_ARG;
+  return level_call(net, packed, points, index, n_dev, n, S, G, 1, store_mode, band, precision,
+                    stream);
 }
 
 extern "C" const char* mpl_status_string(int status) {

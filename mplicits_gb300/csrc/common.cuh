@@ -42,7 +42,7 @@ __device__ __forceinline__ void report_device_error(int* status, int code) {
 
 // Iteration cap of every spin-wait (each try_wait itself may suspend for a
 // bounded hardware time slice, so this is seconds of wall time at most).
-constexpr uint32_t kSpinLimit = 1u << 24;
+constexpr uint32_t kSpinLimit = 1u << 22;
 
 int sm_count();
 

@@ -21,6 +21,8 @@ struct LevelArgs {
   int32_t* band_count;
   int64_t band_capacity;
   int* status;  // device status word
+  int32_t grad;  // also compute df/dx (forward mode) into G
+  float* G;      // [*, 3] gradients, indexed like S (nullable in grad mode)
 };
 
 __device__ __forceinline__ int64_t level_point_count(const LevelArgs& a) {

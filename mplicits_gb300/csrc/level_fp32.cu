@@ -1,10 +1,18 @@
 // Plain-form fused level evaluator: one SIREN level (i3d/model.py:88-129)
 // over a point tile, FP32 SIMT FMAs, accurate sinf.  One CTA per SM; a tile
-// is 128 points x the padded width WP; activations stay in shared memory
+// is 128 rows x the padded width WP; activations stay in shared memory
 // between layers; hidden-layer weights are streamed from L2 as 32-row
 // K-chunks by the TMA engine into a double buffer.  Replaces the per-layer
 // nn.Linear/addmm + SineLayer kernels of the reference and fuses the band
 // test of i3d/meshing.py:223.
+//
+// GRAD mode also returns df/dx by forward-mode differentiation: a tile is
+// 32 points x 4 rows (the value and its three tangents d/dx, d/dy, d/dz);
+// the hidden GEMMs are unchanged, the epilogue of a tangent row is
+// t' = omega cos(z) * (W t), and the output layer dots every row with W_L.
+// This replaces the reference's forward-mode Normals GEMM chains
+// (renderer/cuda/gemms.cu:206-337 with kernels.cu:277-313), which run three
+// separate passes per level.
 #include "level.cuh"
 
 namespace mpl {
@@ -26,8 +34,9 @@ struct Fp32Smem {
   }
 };
 
-template <int WP>
+template <int WP, bool GRAD>
 __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs a) {
+  constexpr int PT = GRAD ? kTile / 4 : kTile;  // points per tile
   constexpr int FPT = WP / 16;
   constexpr int NQ = FPT / 4;  // float4 groups of features per thread
   constexpr int CPL = WP / kKC;  // chunks per hidden layer
@@ -50,7 +59,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
   const float4* act4 = reinterpret_cast<const float4*>(act);
 
   const int64_t n = level_point_count(a);
-  const int64_t ntiles = (n + kTile - 1) / kTile;
+  const int64_t ntiles = (n + PT - 1) / PT;
   if ((int64_t)blockIdx.x >= ntiles) return;
   const int64_t my_tiles = (ntiles - 1 - blockIdx.x) / gridDim.x + 1;
   const int64_t cpt = (int64_t)nh * CPL;  // chunks per tile
@@ -94,8 +103,8 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
 
   for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
     // ---- points of this tile
-    if (tid < kTile) {
-      const int64_t q = t * kTile + tid;
+    if (tid < PT) {
+      const int64_t q = t * PT + tid;
       int64_t p = -1;
       float x = 0.f, y = 0.f, z = 0.f;
       if (q < n) load_point(a, q, p, x, y, z);
@@ -109,14 +118,20 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
     // ---- layer 0: acc = W0 x (+ b0 in the epilogue)
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const int pt = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+      const int row = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+      const int pt = GRAD ? row >> 2 : row;
+      const int ch = GRAD ? (i & 3) : 0;  // 0: value row, 1..3: d/dx_(ch-1)
       const float x = pts[pt * 3 + 0], y = pts[pt * 3 + 1], z = pts[pt * 3 + 2];
 #pragma unroll
       for (int f = 0; f < FPT; ++f) {
         const int j = tx * 4 + (f & 3) + 64 * (f >> 2);
-        float s = __fmul_rn(x, w0t[j]);
-        s = __fmaf_rn(y, w0t[WP + j], s);
-        acc[i][f] = __fmaf_rn(z, w0t[2 * WP + j], s);
+        if (ch == 0) {
+          float s = __fmul_rn(x, w0t[j]);
+          s = __fmaf_rn(y, w0t[WP + j], s);
+          acc[i][f] = __fmaf_rn(z, w0t[2 * WP + j], s);
+        } else {
+          acc[i][f] = w0t[(ch - 1) * WP + j];
+        }
       }
     }
 
@@ -172,8 +187,20 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
           const int j = tx * 4 + (f & 3) + 64 * (f >> 2);
           const float bj = bias[j];
           float s[8];
+          if (GRAD) {
 #pragma unroll
-          for (int i = 0; i < 8; ++i) s[i] = sinf(__fmul_rn(om, __fadd_rn(acc[i][f], bj)));
+            for (int gq = 0; gq < 2; ++gq) {
+              float sv, cv;
+              sincosf(__fmul_rn(om, __fadd_rn(acc[4 * gq][f], bj)), &sv, &cv);
+              cv = __fmul_rn(om, cv);
+              s[4 * gq] = sv;
+#pragma unroll
+              for (int k = 1; k < 4; ++k) s[4 * gq + k] = __fmul_rn(cv, acc[4 * gq + k][f]);
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s[i] = sinf(__fmul_rn(om, __fadd_rn(acc[i][f], bj)));
+          }
           actw[j * (kTile / 4) + ty] = make_float4(s[0], s[1], s[2], s[3]);
           actw[j * (kTile / 4) + 16 + ty] = make_float4(s[4], s[5], s[6], s[7]);
         }
@@ -187,9 +214,22 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
         for (int f = 0; f < FPT; ++f) {
           const int j = tx * 4 + (f & 3) + 64 * (f >> 2);
           const float bj = bias[j], wj = wout[j];
+          if (GRAD) {
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
-            part[i] = __fmaf_rn(sinf(__fmul_rn(om, __fadd_rn(acc[i][f], bj))), wj, part[i]);
+            for (int gq = 0; gq < 2; ++gq) {
+              float sv, cv;
+              sincosf(__fmul_rn(om, __fadd_rn(acc[4 * gq][f], bj)), &sv, &cv);
+              cv = __fmul_rn(om, cv);
+              part[4 * gq] = __fmaf_rn(sv, wj, part[4 * gq]);
+#pragma unroll
+              for (int k = 1; k < 4; ++k)
+                part[4 * gq + k] = __fmaf_rn(__fmul_rn(cv, acc[4 * gq + k][f]), wj, part[4 * gq + k]);
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+              part[i] = __fmaf_rn(sinf(__fmul_rn(om, __fadd_rn(acc[i][f], bj))), wj, part[i]);
+          }
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -199,8 +239,9 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
         if (tx == 0) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const int pt = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
-            fout[pt] = __fadd_rn(part[i], bout);
+            const int row = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+            const bool value_row = !GRAD || (i & 3) == 0;
+            fout[row] = value_row ? __fadd_rn(part[i], bout) : part[i];
           }
         }
         __syncthreads();
@@ -209,9 +250,21 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
     if (!ok) break;
 
     // ---- store / accumulate + fused band compaction
-    if (tid < kTile) {
-      const int64_t q = t * kTile + tid;
-      store_and_band(a, q < n, pidx[tid], fout[tid]);
+    if (tid < PT) {
+      const int64_t q = t * PT + tid;
+      if (GRAD) {
+        const int64_t p = pidx[tid];
+        if (q < n && a.G) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float gk = fout[4 * tid + 1 + k];
+            a.G[3 * p + k] = a.store_mode == MPL_ACCUMULATE ? __fadd_rn(a.G[3 * p + k], gk) : gk;
+          }
+        }
+        store_and_band(a, q < n, p, fout[4 * tid]);
+      } else {
+        store_and_band(a, q < n, pidx[tid], fout[tid]);
+      }
     }
     __syncthreads();
   }
@@ -221,31 +274,37 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
   }
 }
 
-template <int WP>
+template <int WP, bool GRAD>
 int launch_fp32_wp(const LevelArgs& a, cudaStream_t s) {
+  constexpr int PT = GRAD ? kTile / 4 : kTile;
   const size_t smem = Fp32Smem<WP>::bytes(a.lay.nh);
-  MPL_CUDA_TRY(cudaFuncSetAttribute(level_fp32_kernel<WP>,
+  MPL_CUDA_TRY(cudaFuncSetAttribute(level_fp32_kernel<WP, GRAD>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t grid = sm_count();
   if (!a.n_dev) {
-    const int64_t ntiles = (a.n + kTile - 1) / kTile;
+    const int64_t ntiles = (a.n + PT - 1) / PT;
     grid = ntiles < grid ? ntiles : grid;
   }
   if (grid <= 0) return MPL_OK;
-  level_fp32_kernel<WP><<<(unsigned)grid, kThreads, smem, s>>>(a);
+  level_fp32_kernel<WP, GRAD><<<(unsigned)grid, kThreads, smem, s>>>(a);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
+}
+
+template <bool GRAD>
+int launch_fp32_mode(const LevelArgs& a, cudaStream_t s) {
+  switch (a.lay.WP) {
+    case 64: return launch_fp32_wp<64, GRAD>(a, s);
+    case 128: return launch_fp32_wp<128, GRAD>(a, s);
+    case 256: return launch_fp32_wp<256, GRAD>(a, s);
+    default: return MPL_ERR_UNSUPPORTED;
+  }
 }
 
 }  // namespace
 
 int launch_level_fp32(const LevelArgs& a, cudaStream_t s) {
-  switch (a.lay.WP) {
-    case 64: return launch_fp32_wp<64>(a, s);
-    case 128: return launch_fp32_wp<128>(a, s);
-    case 256: return launch_fp32_wp<256>(a, s);
-    default: return MPL_ERR_UNSUPPORTED;
-  }
+  return a.grad ? launch_fp32_mode<true>(a, s) : launch_fp32_mode<false>(a, s);
 }
 
 }  // namespace mpl

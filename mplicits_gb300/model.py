@@ -108,7 +108,7 @@ class _LevelForward(torch.autograd.Function):
     def backward(ctx, gy):
         from . import grad as _grad
         x, *params = ctx.saved_tensors
-        return (None, None) + _grad.level_backward(ctx.model, x, gy, params, ctx.needs_input_grad)
+        return _grad.level_backward(ctx.model, x, gy, params, ctx.needs_input_grad)
 
 
 def level_forward(model, x, S=None, accumulate=False, precision=None):

@@ -130,3 +130,27 @@ def params_from_state_dict(sd):
         b = np.asarray(sd[keys[i + 1]], np.float32)
         params.append((W, b))
     return params
+
+
+def multistage_sdf_threaded(levels, deltas, N, index, threads, chunk=32 ** 3):
+    """``multistage_sdf`` over ``index`` with the chunks spread over a thread
+    pool (numpy releases the GIL in matmul and sin).  Used to time the CPU
+    baseline on the host's cores; with OPENBLAS_NUM_THREADS=1 each chunk is
+    single-threaded and the pool provides the parallelism."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    index = np.asarray(index, np.int64)
+    heads = list(range(0, index.shape[0], chunk))
+    out = np.empty(index.shape[0], np.float32)
+    band_sizes = np.zeros((len(heads), max(len(levels) - 1, 1)), np.int64)
+
+    def work(t):
+        head = heads[t]
+        S, bands = multistage_sdf(levels, deltas, N, chunk=chunk, index=index[head:head + chunk])
+        out[head:head + chunk] = S
+        for i, b in enumerate(bands):
+            band_sizes[t, i] = b.shape[0]
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(work, range(len(heads))))
+    return out, band_sizes.sum(0)

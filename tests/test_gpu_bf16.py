@@ -1,0 +1,93 @@
+"""BF16 tcgen05 level kernel: exactness of the tensor-core arithmetic
+(against a numpy emulation of the same BF16 roundings) and its error
+against the FP64 oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import siren
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_round(a):
+    """Round float32 values to bfloat16 (nearest even), returned as float64."""
+    a = np.asarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def emulate_bf16_level(params, omegas, x):
+    """The kernel's arithmetic in float64: FP32-phase layer 0 with omega
+    folded, BF16 activations and BF16 omega*W in the hidden GEMMs, FP32
+    sines into the output layer."""
+    W0, b0 = params[0]
+    z = np.asarray(x, np.float64) @ (omegas[0] * W0.astype(np.float64)).T + omegas[0] * b0
+    s = np.sin(z)
+    for l in range(1, len(params) - 1):
+        W, b = params[l]
+        Wq = bf16_round(np.float32(omegas[l]) * W.astype(np.float32))
+        z = bf16_round(s.astype(np.float32)) @ Wq.T + omegas[l] * b.astype(np.float64)
+        s = np.sin(z)
+    Wl, bl = params[-1]
+    return (s @ Wl.astype(np.float64).T + bl)[:, 0]
+
+
+def _model(cfg, seed):
+    from mplicits_gb300.model import SIREN
+    torch.manual_seed(seed)
+    m = SIREN(3, 1, cfg, w0=30, precision="bf16").cuda().eval()
+    params = siren.params_from_state_dict({k: v.cpu().numpy() for k, v in m.state_dict().items()})
+    return m, params
+
+
+@pytest.mark.parametrize("cfg", [[256, 256, 256], [128, 128, 128], [64, 64], [100, 60, 17],
+                                 [256, 256, 256, 256, 256]])
+@pytest.mark.parametrize("P", [1, 200, 20000])
+def test_bf16_tensor_core_arithmetic_is_exact(lib, cfg, P):
+    from mplicits_gb300.model import level_forward
+    m, params = _model(cfg, 7 + len(cfg))
+    rng = np.random.default_rng(P)
+    x = rng.uniform(-1, 1, (P, 3)).astype(np.float32)
+    out = level_forward(m, torch.from_numpy(x).cuda(), precision="bf16").cpu().numpy()
+    emu = emulate_bf16_level(params, m.omegas(), x)
+    # exact up to accumulation order and the fast sine; a BF16 rounding
+    # boundary flip of an activation moves a rare point by up to ~1e-3
+    err = np.abs(out - emu)
+    if P >= 100:
+        assert np.median(err) <= 1e-6
+    assert err.max() <= 1e-3
+    from mplicits_gb300 import capi
+    assert capi.device_status() == capi.MPL_OK
+
+
+def test_bf16_error_against_fp64_oracle_cfg1(lib):
+    from mplicits_gb300.model import level_forward
+    m, params = _model([256, 256, 256], 0)
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, (1 << 16, 3)).astype(np.float32)
+    out = level_forward(m, torch.from_numpy(x).cuda(), precision="bf16").cpu().numpy()
+    ref = siren.siren_forward(params, m.omegas(), x, np.float64)
+    err = np.abs(out - ref)
+    print(f"bf16 vs fp64: max {err.max():.3e} rms {np.sqrt((err ** 2).mean()):.3e}")
+    assert err.max() <= 5e-3
+
+
+def test_bf16_grid_band_pipeline_matches_fp32_bands_where_clear(lib):
+    """Grid mode + fused band in BF16: every point whose BF16 value is
+    farther than the error margin from delta gets the FP32 decision."""
+    from mplicits_gb300.meshing import BandedReconstruction
+    m, params = _model([256, 256, 256], 3)
+    rec32 = BandedReconstruction([m, m], [0.05], 48, "cuda", precision="fp32")
+    rec16 = BandedReconstruction([m, m], [0.05], 48, "cuda", precision="bf16")
+    rec32.sample()
+    rec16.sample()
+    S0 = BandedReconstruction([m], [], 48, "cuda", precision="fp32").sample().cpu().numpy()
+    k32 = rec32.band_sizes()[0]
+    k16 = rec16.band_sizes()[0]
+    b32 = set(rec32.band_index[0][:k32].cpu().tolist())
+    b16 = set(rec16.band_index[0][:k16].cpu().tolist())
+    diff = b32 ^ b16
+    assert all(abs(abs(S0[p]) - 0.05) < 5e-3 for p in diff)

@@ -1,0 +1,79 @@
+"""Sphere tracing: the camera against the reference's ray tests (CPU) and the
+GPU tracer against the numpy restatement."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import trace as otrace
+
+
+def _cam(eye, W=800, H=600, fov=45.0):
+    return dict(eye=eye, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov=fov, width=W, height=H)
+
+
+def test_camera_matches_reference_ray_test():
+    """renderer/cuda/tests/tests.cu:89-135: 800x600, 45 degrees, eye
+    (2, 1, 5) looking at the origin."""
+    cam = _cam((2.0, 1.0, 5.0))
+    o, d, state = otrace.camera_rays(cam, radius=100.0)
+    W, H = 800, 600
+    center = d[(H // 2) * W + W // 2]
+    expected = -np.array([2.0, 1.0, 5.0]) / np.linalg.norm([2.0, 1.0, 5.0])
+    assert np.abs(center - expected).max() < 0.01
+    tl, br = d[0], d[(H - 1) * W + (W - 1)]
+    assert tl[0] < 0 and tl[1] > 0 and tl[2] < -0.5
+    assert br[0] > 0 and br[1] < 0 and br[2] < -0.5
+
+
+def test_orbit_cameras_are_seeded_and_on_the_orbit():
+    from mplicits_gb300.trace import orbit_cameras
+    a, b = orbit_cameras(), orbit_cameras()
+    assert a == b and len(a) == 8
+    for c in a:
+        assert abs(np.linalg.norm(c["eye"]) - 2.5) < 1e-9
+
+
+def _sphere_levels():
+    """Three small levels whose sum is close to a sphere SDF of radius 0.5:
+    level 0 is a trained-free analytic stand-in built from SIREN weights
+    that make f0(x) ~ 0.5*sin(...) small; instead use random small levels."""
+    from mplicits_gb300.model import SIREN
+    levels = []
+    for seed, scale in ((0, 1.0), (1, 0.05), (2, 0.01)):
+        torch.manual_seed(seed)
+        m = SIREN(3, 1, [64, 64], w0=30)
+        with torch.no_grad():
+            m.net[-1][0].weight.mul_(scale)
+            m.net[-1][0].bias.mul_(scale)
+        levels.append(m)
+    return levels
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [False, True])
+def test_gpu_tracer_matches_oracle(lib, graph):
+    from mplicits_gb300.trace import SphereTracer
+    from oracle import siren
+    levels = [m.cuda().eval() for m in _sphere_levels()]
+    params = [(siren.params_from_state_dict({k: v.cpu().numpy() for k, v in m.state_dict().items()}),
+               m.omegas()) for m in levels]
+    deltas = [0.05, 0.01]
+    cam = _cam((0.3, 0.4, 2.5), W=96, H=64)
+    tr = SphereTracer(levels, deltas, 96, 64, max_steps=48, eps=1e-3, precision="fp32",
+                      graph=graph)
+    img, state = tr.render(cam)
+    torch.cuda.synchronize()
+    o_ref, s_ref, g_ref = otrace.trace(params, deltas, cam, max_steps=48, eps=1e-3)
+    st = state.cpu().numpy()
+    agree = (st == s_ref).mean()
+    assert agree >= 0.97, agree
+    both = (st == 1) & (s_ref == 1)
+    assert both.sum() > 50
+    org = tr.org.cpu().numpy()
+    assert np.median(np.abs(org[both] - o_ref[both]).max(1)) <= 1e-4
+    G = tr.G.cpu().numpy()
+    cos = (G[both] * g_ref[both]).sum(1) / (np.linalg.norm(G[both], axis=1) *
+                                           np.linalg.norm(g_ref[both], axis=1))
+    assert np.median(cos) > 0.9999
+    assert img.shape == (64, 96)
