@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--cpu-slabs", type=int, default=16, help="grid slabs timed on the CPU")
     ap.add_argument("--skip-errors", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="time only the BF16 steps (for profiler runs) and print a short line")
     return ap.parse_args()
 
 
@@ -411,6 +413,11 @@ def main():
         ms = float(t)
     value = world * N ** 3 / (ms * 1e-3)
     bands = bf16.rec.band_sizes()
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "ms_per_step": ms, "level0_ms": l0_ms,
+                              "value": value, "grid": N, "band_points": bands}), flush=True)
+        return
 
     # ---- plain FP32 kernels, same step
     fp32 = Step(make_models(levels_np, "fp32", device), N, device, "fp32")
