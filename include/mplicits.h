@@ -175,6 +175,26 @@ int mpl_mc_emit(const float* S_dev, int64_t N, float iso, float voxel_size,
                 float* normals_dev, float* values_dev, int32_t* faces_dev, int64_t max_verts,
                 int64_t max_tris, void* stream);
 
+/* Marching cubes in one call that allocates nothing.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory, such
+ * as a real-time frame loop that must not pay the device-wide
+ * synchronisation of cudaMalloc/cudaFree, or a host program that can only
+ * pass buffers it registered itself.  The count/prefix workspace lives in a
+ * fixed device array inside the library (1.5 MiB, held on every GPU that
+ * loads the library until exit), so N is limited to 256; a larger N returns
+ * MPL_ERR_CAPACITY.  The first call on each device does one-time set-up
+ * (it looks up the array's device address and uploads the case tables);
+ * make that first call before any stream capture.  Calls that overlap on
+ * the GPU share the
+ * array and race: order them on one stream.  Output as mpl_mc_emit, with
+ * counts_dev[0], [1] = the full vertex and triangle counts (int64); output
+ * beyond max_verts / max_tris is dropped, so counts above the capacities
+ * mean the mesh was cut short. */
+int mpl_mc_noalloc(const float* S_dev, int64_t N, float iso, float voxel_size,
+                   const float* origin_host, float* verts_dev, float* normals_dev,
+                   float* values_dev, int32_t* faces_dev, int64_t max_verts, int64_t max_tris,
+                   int64_t* counts_dev, void* stream);
+
 /* ---- sphere tracing (renderer/cuda/kernels.cu:315-487, state.cu:848-880) */
 
 /* Generates one ray per pixel into origins/dirs [W*H, 3], moves every origin

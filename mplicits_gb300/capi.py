@@ -83,6 +83,7 @@ SIGNATURES = {
     "mpl_mc_workspace_bytes": (ctypes.c_int, [_I64, ctypes.POINTER(_I64)]),
     "mpl_mc_count": (ctypes.c_int, [_P, _I64, _F, _P, _P, _P]),
     "mpl_mc_emit": (ctypes.c_int, [_P, _I64, _F, _F, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
+    "mpl_mc_noalloc": (ctypes.c_int, [_P, _I64, _F, _F, _P, _P, _P, _P, _P, _I64, _I64, _P, _P]),
     "mpl_trace_init": (ctypes.c_int, [ctypes.POINTER(MplCamera), _F, _P, _P, _P, _P, _P, _P]),
     "mpl_trace_step": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _F, _F, _I32, _P, _P, _P, _P,
                                       _I64, _P]),

@@ -392,3 +392,87 @@ extern "C" int mpl_mc_emit(const float* S, int64_t N, float iso, float voxel_siz
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Marching cubes without any allocation, for callers that cannot allocate
+// device memory.  A real-time frame loop cannot afford cudaMalloc/cudaFree,
+// which synchronise the whole device, and a host that hands this library
+// only buffers it registered itself (an engine plug-in, or a foreign-language
+// binding without access to a CUDA allocator) has no way to provide the
+// workspace mpl_mc_count/mpl_mc_emit need.  This entry point keeps that
+// workspace in a fixed file-scope device array instead, sized for grids up
+// to kStaticMaxN^3, which every GPU that loads the library holds until the
+// process exits.
+// ---------------------------------------------------------------------------
+namespace mpl {
+
+namespace {
+
+constexpr int64_t kStaticMaxN = 256;
+
+constexpr int64_t static_align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+constexpr int64_t static_ws_bytes(int64_t N) {
+  return static_align256(N * N * 4) * 2 + static_align256(N * N * 8) * 2 +
+         static_align256(2 * ((N * N + kScanChunk - 1) / kScanChunk) * 8) + 256;
+}
+
+// 1.5 MiB: the count/prefix workspace of a 256^3 grid.
+__device__ __align__(256) unsigned char g_mc_static_ws[static_ws_bytes(kStaticMaxN)];
+
+// Device address of g_mc_static_ws on the current device.  In host code the
+// symbol itself is only a host-side stand-in, so the address is looked up
+// once per device (with that device current) and cached.
+int static_ws_address(void** out) {
+  static void* cached[64] = {nullptr};
+  int dev = 0;
+  MPL_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return MPL_ERR_INVALID_ARG;
+  if (!cached[dev]) {
+    void* p = nullptr;
+    MPL_CUDA_TRY(cudaGetSymbolAddress(&p, g_mc_static_ws));
+    cached[dev] = p;
+  }
+  *out = cached[dev];
+  return MPL_OK;
+}
+
+}  // namespace
+
+}  // namespace mpl
+
+extern "C" int mpl_mc_noalloc(const float* S, int64_t N, float iso, float voxel_size,
+                              const float* origin, float* verts, float* normals, float* values,
+                              int32_t* faces, int64_t max_verts, int64_t max_tris,
+                              int64_t* counts_dev, void* stream) {
+  if (!S || !origin || !counts_dev || N < 2) return MPL_ERR_INVALID_ARG;
+  if (N > kStaticMaxN || mc_work_bytes(N) > (int64_t)sizeof(g_mc_static_ws))
+    return MPL_ERR_CAPACITY;
+  if (max_verts < 0 || max_tris < 0) return MPL_ERR_INVALID_ARG;
+  if ((max_verts > 0 && (!verts || !normals)) || (max_tris > 0 && !faces))
+    return MPL_ERR_INVALID_ARG;
+  int st = ensure_tables();
+  if (st != MPL_OK) return st;
+  void* ws = nullptr;
+  st = static_ws_address(&ws);
+  if (st != MPL_OK) return st;
+  // Every workspace entry the kernels read is written earlier in this same
+  // call, so the previous call's leftovers need no clearing.
+  cudaStream_t s = (cudaStream_t)stream;
+  McWork w = mc_work(ws, N);
+  const int64_t R = N * N;
+  mc_count_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(S, N, iso, w);
+  MPL_LAUNCH_CHECK();
+  const int64_t nblk = mc_nblk(N);
+  mc_scan_blocks<<<(unsigned)nblk, 256, 0, s>>>(N, w);
+  MPL_LAUNCH_CHECK();
+  mc_scan_top<<<1, 256, 0, s>>>(nblk, w, counts_dev);
+  MPL_LAUNCH_CHECK();
+  mc_scan_add<<<(unsigned)((R + 255) / 256), 256, 0, s>>>(N, w);
+  MPL_LAUNCH_CHECK();
+  mc_emit_kernel<<<(unsigned)R, kEmitThreads, 0, s>>>(S, N, iso, voxel_size, origin[0],
+                                                       origin[1], origin[2], w, verts, normals,
+                                                       values, faces, max_verts, max_tris);
+  MPL_LAUNCH_CHECK();
+  return MPL_OK;
+}
