@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--cpu-slabs", type=int, default=16, help="grid slabs timed on the CPU")
     ap.add_argument("--skip-errors", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--bf16-unit", type=int, default=None, choices=[16, 32],
+                    help="epilogue unit width of the BF16 kernel (default: the library's)")
     ap.add_argument("--profile-only", action="store_true",
                     help="time only the BF16 steps (for profiler runs) and print a short line")
     return ap.parse_args()
@@ -399,6 +401,9 @@ def main():
     __graft_entry__.build()
     N, K, W = args.N, args.steps, max(3, args.warmup)
     levels_np = load_levels_np()
+    from mplicits_gb300 import capi
+    if args.bf16_unit:
+        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, args.bf16_unit)
 
     # ---- BF16 fused (the headline)
     bf16 = Step(make_models(levels_np, "bf16", device), N, device, "bf16")

@@ -226,6 +226,17 @@ int mpl_trace_shade(const float* origins_dev, const float* dirs_dev, const float
                     const int32_t* state_dev, int64_t P, int32_t mode, uint32_t* image_dev,
                     void* stream);
 
+/* ---- tuning ------------------------------------------------------------- */
+
+/* Process-wide kernel options (read at each launch). */
+enum {
+  MPL_OPT_BF16_EPILOGUE_UNIT = 1 /* features per epilogue warp and 64-wide chunk of
+                                    the BF16 level kernel: 16 (16 epilogue warps,
+                                    default) or 32 (8 warps)                     */
+};
+int mpl_set_option(int32_t option, int64_t value);
+int mpl_get_option(int32_t option, int64_t* value);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 const char* mpl_status_string(int status);

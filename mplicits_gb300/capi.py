@@ -31,6 +31,7 @@ MPL_POINTS_XYZ = 0
 MPL_POINTS_GRID = 1
 
 PRECISIONS = {"fp32": MPL_FP32, "bf16": MPL_BF16}
+MPL_OPT_BF16_EPILOGUE_UNIT = 1
 
 
 class MplNet(ctypes.Structure):
@@ -88,6 +89,8 @@ SIGNATURES = {
     "mpl_trace_step": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _F, _F, _I32, _P, _P, _P, _P,
                                       _I64, _P]),
     "mpl_trace_shade": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P]),
+    "mpl_set_option": (ctypes.c_int, [_I32, _I64]),
+    "mpl_get_option": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
     "mpl_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "mpl_device_status": (ctypes.c_int, [ctypes.POINTER(_I32)]),
     "mpl_last_cuda_error": (ctypes.c_int, []),
@@ -154,4 +157,14 @@ def device_status():
     """Synchronise and read/clear the device status word (MPL_OK if clean)."""
     v = _I32(0)
     check(load().mpl_device_status(ctypes.byref(v)), "mpl_device_status")
+    return v.value
+
+
+def set_option(option, value):
+    check(load().mpl_set_option(option, value), "mpl_set_option")
+
+
+def get_option(option):
+    v = _I64(0)
+    check(load().mpl_get_option(option, ctypes.byref(v)), "mpl_get_option")
     return v.value

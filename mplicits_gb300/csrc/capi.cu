@@ -35,9 +35,36 @@ int sm_count() {
   return cached[dev];
 }
 
+static int64_t g_opt_bf16_unit = 16;
+
+int64_t option_value(int32_t option) {
+  switch (option) {
+    case MPL_OPT_BF16_EPILOGUE_UNIT: return g_opt_bf16_unit;
+    default: return 0;
+  }
+}
+
 }  // namespace mpl
 
 using namespace mpl;
+
+extern "C" int mpl_set_option(int32_t option, int64_t value) {
+  switch (option) {
+    case MPL_OPT_BF16_EPILOGUE_UNIT:
+      if (value != 16 && value != 32) return MPL_ERR_INVALID_ARG;
+      g_opt_bf16_unit = value;
+      return MPL_OK;
+    default:
+      return MPL_ERR_INVALID_ARG;
+  }
+}
+
+extern "C" int mpl_get_option(int32_t option, int64_t* value) {
+  if (!value) return MPL_ERR_INVALID_ARG;
+  if (option != MPL_OPT_BF16_EPILOGUE_UNIT) return MPL_ERR_INVALID_ARG;
+  *value = option_value(option);
+  return MPL_OK;
+}
 
 static int level_call(const MplNet* net, const void* packed, const MplPoints* points,
                       const int32_t* index, const int32_t* n_dev, int64_t n, float* S, float* G,

@@ -46,20 +46,23 @@ constexpr uint32_t kSpinLimit = 1u << 22;
 
 int sm_count();
 
+// current value of a process-wide option (mpl_set_option)
+int64_t option_value(int32_t option);
+
 // ---------------------------------------------------------------------------
 // grid coordinates of i3d/meshing.py:42-63 (float32 true division, fmod)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void grid_point(int64_t p, int32_t N, float vs, const float off[3],
-                                           float& x, float& y, float& z) {
+__device__ __forceinline__ void grid_point(int64_t p, int32_t N, float vs, float off0, float off1,
+                                           float off2, float& x, float& y, float& z) {
   const float fN = (float)N;
   const float idx_f = __ll2float_rn(p);
   const float s2 = (float)(p % (int64_t)N);
   const float q1 = __fdiv_rn(idx_f, fN);
   const float s1 = fmodf(q1, fN);
   const float s0 = fmodf(__fdiv_rn(q1, fN), fN);
-  x = __fadd_rn(__fmul_rn(s0, vs), off[0]);
-  y = __fadd_rn(__fmul_rn(s1, vs), off[1]);
-  z = __fadd_rn(__fmul_rn(s2, vs), off[2]);
+  x = __fadd_rn(__fmul_rn(s0, vs), off0);
+  y = __fadd_rn(__fmul_rn(s1, vs), off1);
+  z = __fadd_rn(__fmul_rn(s2, vs), off2);
 }
 
 // ---------------------------------------------------------------------------
@@ -102,6 +105,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// As mbar_try_wait, but the thread may be suspended in hardware for up to
+// hint_ns nanoseconds while the phase is incomplete (it resumes as soon as
+// the phase completes), so a waiting warp does not spin on the issue port.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wall-clock cap of a sleeping wait: far above any legitimate wait inside a
+// launch (microseconds), so only a wait that can never complete reaches it.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
 // Bounded wait for the phase with the given parity to complete.  Returns
 // false (and records MPL_ERR_DEVICE_TIMEOUT) when the cap is reached.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
@@ -142,6 +171,12 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 //         c*WP*128 + ((n/8)*8 + (k%64)/8)*128 + (n%8)*16 + (k%8)*2 bytes.
 //   hwT_l bf16 omega_l*W_l^T, same tiling (rows = input features): used by
 //         the input-gradient kernels.
+//   hbx_l bf16 [WP rows][16 K] bias tile of the MMA: K column 0 holds
+//         bf16(omega_l*b_l), column 1 the bf16 remainder, the rest zero;
+//         core-matrix layout ((n/8)*2 + k/8)*128 + (n%8)*16 + (k%8)*2 bytes
+//         (LBO 128 B, SBO 256 B).  Multiplied by an A tile whose first two
+//         K columns are 1, one extra K=16 MMA step adds the bias exactly to
+//         ~16 bits.
 struct PackLayout {
   int32_t L;    // nn.Linear layers
   int32_t WP;   // padded hidden width (64, 128 or 256)
@@ -150,7 +185,7 @@ struct PackLayout {
   int64_t wht[MPL_MAX_LAYERS], bh[MPL_MAX_LAYERS];
   int64_t w0f;
   int64_t hb[MPL_MAX_LAYERS];
-  int64_t hw[MPL_MAX_LAYERS], hwT[MPL_MAX_LAYERS];
+  int64_t hw[MPL_MAX_LAYERS], hwT[MPL_MAX_LAYERS], hbx[MPL_MAX_LAYERS];
   int64_t total;
 };
 

@@ -11,7 +11,8 @@ __global__ void grid_points_kernel(MplPoints pts, const int32_t* __restrict__ in
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
     const int64_t p = index ? (int64_t)index[q] : q;
     float x, y, z;
-    grid_point(p, pts.grid_n, pts.voxel_size, pts.offset, x, y, z);
+    grid_point(p, pts.grid_n, pts.voxel_size, pts.offset[0], pts.offset[1], pts.offset[2], x,
+               y, z);
     out[3 * q + 0] = x;
     out[3 * q + 1] = y;
     out[3 * q + 2] = z;

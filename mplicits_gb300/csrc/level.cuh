@@ -38,7 +38,8 @@ __device__ __forceinline__ void load_point(const LevelArgs& a, int64_t q, int64_
                                            float& y, float& z) {
   p = a.index ? (int64_t)a.index[q] : q;
   if (a.pts.kind == MPL_POINTS_GRID) {
-    grid_point(p, a.pts.grid_n, a.pts.voxel_size, a.pts.offset, x, y, z);
+    grid_point(p, a.pts.grid_n, a.pts.voxel_size, a.pts.offset[0], a.pts.offset[1],
+               a.pts.offset[2], x, y, z);
   } else {
     x = a.pts.xyz[3 * p + 0];
     y = a.pts.xyz[3 * p + 1];

@@ -30,7 +30,7 @@ int make_layout(const MplNet* net, PackLayout* lay) {
   lay->w0t = take(3 * WP * 4);
   lay->b0 = take(WP * 4);
   for (int l = 0; l < MPL_MAX_LAYERS; ++l) {
-    lay->wht[l] = lay->bh[l] = lay->hb[l] = lay->hw[l] = lay->hwT[l] = -1;
+    lay->wht[l] = lay->bh[l] = lay->hb[l] = lay->hw[l] = lay->hwT[l] = lay->hbx[l] = -1;
   }
   for (int l = 1; l <= L - 2; ++l) {
     lay->wht[l] = take((int64_t)WP * WP * 4);
@@ -43,6 +43,7 @@ int make_layout(const MplNet* net, PackLayout* lay) {
     lay->hb[l] = take(WP * 4);
     lay->hw[l] = take((int64_t)WP * WP * 2);
     lay->hwT[l] = take((int64_t)WP * WP * 2);
+    lay->hbx[l] = take((int64_t)WP * 16 * 2);
   }
   lay->total = o;
   return MPL_OK;
@@ -84,6 +85,21 @@ __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict
     bh[n] = bb;
     hb[n] = omega * bb;
   }
+}
+
+// bias tile of the MMA (see PackLayout::hbx): row n, K columns 0 and 1
+__global__ void pack_bias_tile(const float* __restrict__ b, int out, int WP, float omega,
+                               __nv_bfloat16* hbx) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= WP) return;
+  const float v = n < out ? omega * b[n] : 0.f;
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+  const int base = ((n >> 3) * 2) * 64 + (n & 7) * 8;  // elements; K group 0
+  for (int k = 0; k < 8; ++k) hbx[base + k] = __float2bfloat16_rn(0.f);
+  for (int k = 0; k < 8; ++k) hbx[base + 64 + k] = __float2bfloat16_rn(0.f);
+  hbx[base + 0] = hi;
+  hbx[base + 1] = lo;
 }
 
 __global__ void pack_output(const float* __restrict__ W, const float* __restrict__ b, int in,
@@ -132,6 +148,10 @@ extern "C" int mpl_net_pack(const MplNet* net, const float* const* weights,
         weights[l], biases[l], net->dims[l + 1], net->dims[l], WP, net->omega[l],
         (float*)(base + lay.wht[l]), (float*)(base + lay.bh[l]), (float*)(base + lay.hb[l]),
         (__nv_bfloat16*)(base + lay.hw[l]), (__nv_bfloat16*)(base + lay.hwT[l]));
+    MPL_LAUNCH_CHECK();
+    pack_bias_tile<<<(WP + 127) / 128, 128, 0, s>>>(biases[l], net->dims[l + 1], WP,
+                                                    net->omega[l],
+                                                    (__nv_bfloat16*)(base + lay.hbx[l]));
     MPL_LAUNCH_CHECK();
   }
   pack_output<<<(WP + 127) / 128, 128, 0, s>>>(weights[lay.L - 1], biases[lay.L - 1],

@@ -42,8 +42,11 @@ def test_fp32_gradient_vs_fp64(lib, cfg, P):
     assert np.abs(S.cpu().numpy() - siren.siren_forward(params, m.omegas(), x, np.float64)).max() <= 1e-5
 
 
+@pytest.mark.parametrize("unit", [16, 32])
 @pytest.mark.parametrize("cfg", [[256, 256, 256], [128, 128, 128], [64, 64]])
-def test_bf16_gradient_vs_fp64(lib, cfg):
+def test_bf16_gradient_vs_fp64(lib, cfg, unit):
+    from mplicits_gb300 import capi
+    capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, unit)
     from mplicits_gb300.grad import level_gradient
     m, params = _model(cfg, 5, precision="bf16")
     x = np.random.default_rng(9).uniform(-1, 1, (20000, 3)).astype(np.float32)
@@ -54,8 +57,8 @@ def test_bf16_gradient_vs_fp64(lib, cfg):
     assert np.median(err) <= 2e-2
     f64 = siren.siren_forward(params, m.omegas(), x, np.float64)
     assert np.abs(S.cpu().numpy() - f64).max() <= 5e-3
-    from mplicits_gb300 import capi
     assert capi.device_status() == capi.MPL_OK
+    capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 16)
 
 
 def test_autograd_input_gradient_through_forward(lib):
