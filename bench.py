@@ -41,6 +41,9 @@ METRIC = ("fused BF16 vs plain FP32 SDF pts/s & 512³ banded-MC ms on 1 GB300 "
           "at equal error")
 WEIGHTS = os.path.join(ROOT, "tests", "golden", "three_level_sphere.npz")
 DELTAS = [0.05, 0.01]
+# FP32 re-evaluation margins: about four times the largest tensor-core error
+# of a partial sum measured near the surface (BF16 ~5e-4, FP16 ~2.5e-4)
+REFINE = {"bf16": 2e-3, "fp16": 1e-3}
 FLOP_PER_POINT = 2 * (3 * 256 + 256 * 256 * 2 + 256)  # 264,192 per level evaluation
 KERNEL_LAUNCHES_PER_STEP = 3 + 5  # 3 level launches; MC count, 3 scan passes, emit
 
@@ -146,10 +149,10 @@ def make_models(levels_np, precision, device):
 class Step:
     """One band-culled reconstruction on resident weights, no host sync."""
 
-    def __init__(self, models, N, device, precision):
+    def __init__(self, models, N, device, precision, refine_margin=None):
         import torch
         from mplicits_gb300.meshing import BandedReconstruction, MarchingCubes
-        self.rec = BandedReconstruction(models, DELTAS, N, device, precision)
+        self.rec = BandedReconstruction(models, DELTAS, N, device, precision, refine_margin)
         self.mc = MarchingCubes(N, device)
         for m in models:
             m.packed()
@@ -168,7 +171,7 @@ class Step:
         import ctypes
         from mplicits_gb300 import capi
         rec = self.rec
-        if l0_events is not None:
+        if l0_events is not None and not rec.refine_margin:
             l0_events[0].record()
             self._level(0)
             l0_events[1].record()
@@ -221,7 +224,8 @@ def time_steps(step, K, W, with_l0=True):
     e1.record()
     torch.cuda.synchronize()
     total_ms = e0.elapsed_time(e1)
-    l0_ms = float(np.mean([a.elapsed_time(b) for a, b in l0])) if with_l0 else None
+    l0_ms = (float(np.mean([a.elapsed_time(b) for a, b in l0]))
+             if with_l0 and not step.rec.refine_margin else None)
     return total_ms / K, l0_ms
 
 
@@ -424,14 +428,32 @@ def main():
                               "value": value, "grid": N, "band_points": bands}), flush=True)
         return
 
-    # ---- plain FP32 kernels, same step
+    # ---- the other arithmetic: FP16 operands, FP32 refinement margins, plain FP32
+    variants = {"bf16": {"ms_per_step": ms, "level0_ms": l0_ms}}
+    steps = {"bf16": bf16}
+    for name, prec, margin in (("fp16", "fp16", None), ("bf16_refined", "bf16", REFINE["bf16"]),
+                               ("fp16_refined", "fp16", REFINE["fp16"])):
+        st = Step(make_models(levels_np, prec, device), N, device, prec, margin)
+        vms, vl0 = time_steps(st, K, W)
+        variants[name] = {"ms_per_step": vms, "level0_ms": vl0, "value": N ** 3 / (vms * 1e-3),
+                          "refine_margin": margin}
+        steps[name] = st
     fp32 = Step(make_models(levels_np, "fp32", device), N, device, "fp32")
     ms32, l0_32 = time_steps(fp32, max(1, args.fp32_steps), 1)
+    steps["fp32"] = fp32
 
     errors = None
     if not args.skip_errors and rank == 0:
-        errors = {"bf16": error_stats(bf16, bf16.rec.levels, N),
-                  "fp32": error_stats(fp32, fp32.rec.levels, N)}
+        errors = {k: error_stats(v, v.rec.levels, N) for k, v in steps.items()}
+        ref_faces = fp32.faces[:fp32.F]
+        for k, v in steps.items():
+            errors[k]["mesh_topology_equals_fp32"] = bool(
+                v.F == fp32.F and torch.equal(v.faces[:v.F], ref_faces))
+        for k in ("bf16_refined", "fp16_refined"):
+            a, b = fp32.rec, steps[k].rec
+            errors[k]["band_lists_equal_fp32"] = all(
+                torch.equal(torch.sort(a.band_index[i][:a.band_sizes()[i]])[0],
+                            torch.sort(b.band_index[i][:b.band_sizes()[i]])[0]) for i in range(2))
 
     # ---- end to end through the public API with host buffers
     e2e_s, h2d, d2h, e2e_launch = e2e_run(levels_np, N, device, max(1, K // 2), 1)
@@ -467,6 +489,7 @@ def main():
                              "and read every step",
                        "parallelism": f"replicas x{world}"},
             "banded_mc_ms": {"bf16_fused": ms, "fp32_plain": ms32},
+            "variants": variants,
             "fp32_plain": {"value": N ** 3 / (ms32 * 1e-3), "unit": "pts/s", "ms_per_step": ms32,
                            "level0_ms": l0_32},
             "speedup_bf16_vs_fp32": ms32 / ms,

@@ -45,7 +45,9 @@ enum {
 /* arithmetic of the hidden-layer GEMMs */
 enum {
   MPL_FP32 = 0, /* plain form: FP32 SIMT FMAs, accurate sinf               */
-  MPL_BF16 = 1  /* tcgen05 BF16 MMAs, FP32 accumulate in TMEM, FP32 layer 0 */
+  MPL_BF16 = 1, /* tcgen05 BF16 MMAs, FP32 accumulate in TMEM, FP32 layer 0 */
+  MPL_F16 = 2   /* the same kernels with FP16 operands: same speed, 8x finer
+                   rounding of the sine activations (all within [-1, 1])   */
 };
 
 /* how a level's output is stored */
@@ -82,15 +84,17 @@ typedef struct MplPoints {
 } MplPoints;
 
 /* Fused band compaction: after a level stores S[p], p is appended to
- * out_index when |S[p]| < delta (float32 compare, i3d/meshing.py:223).
- * *count_dev is reset to 0 by the call.  Entries past `capacity` are dropped
- * but still counted, so *count_dev > capacity reports an overflow.  The
- * order of out_index is unspecified; its set is exact. */
+ * out_index when lower <= |S[p]| < delta (float32 compares; lower = 0 gives
+ * the reference's |S| < delta of i3d/meshing.py:223).  *count_dev is reset
+ * to 0 by the call.  Entries past `capacity` are dropped but still counted,
+ * so *count_dev > capacity reports an overflow.  The order of out_index is
+ * unspecified; its set is exact. */
 typedef struct MplBand {
   float delta;
   int32_t* out_index;  /* device [capacity]                                  */
   int32_t* count_dev;  /* device int32 scalar                                */
   int64_t capacity;
+  float lower;         /* keep only |S| >= lower (0: no lower bound)         */
 } MplBand;
 
 /* A pinhole camera: look-at eye/target/up, vertical field of view, image
@@ -150,7 +154,7 @@ int mpl_level_gradient(const MplNet* net, const void* packed_dev, const MplPoint
 /* ---- band compaction (i3d/meshing.py:222-231) --------------------------- */
 
 /* Appends q's point p = index ? index[q] : q for q < n (or < *n_dev) with
- * |S[p]| < band->delta to band->out_index. */
+ * band->lower <= |S[p]| < band->delta to band->out_index. */
 int mpl_band_compact(const float* S_dev, const int32_t* index_dev, const int32_t* n_dev,
                      int64_t n, const MplBand* band, void* stream);
 

@@ -25,12 +25,13 @@ MPL_ERR_NO_DEVICE = 6
 
 MPL_FP32 = 0
 MPL_BF16 = 1
+MPL_F16 = 2
 MPL_STORE = 0
 MPL_ACCUMULATE = 1
 MPL_POINTS_XYZ = 0
 MPL_POINTS_GRID = 1
 
-PRECISIONS = {"fp32": MPL_FP32, "bf16": MPL_BF16}
+PRECISIONS = {"fp32": MPL_FP32, "bf16": MPL_BF16, "fp16": MPL_F16}
 MPL_OPT_BF16_EPILOGUE_UNIT = 1
 
 
@@ -52,7 +53,8 @@ class MplBand(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_float),
                 ("out_index", ctypes.c_void_p),
                 ("count_dev", ctypes.c_void_p),
-                ("capacity", ctypes.c_int64)]
+                ("capacity", ctypes.c_int64),
+                ("lower", ctypes.c_float)]
 
 
 class MplCamera(ctypes.Structure):

@@ -8,6 +8,7 @@ namespace mpl {
 
 __global__ void band_compact_kernel(const float* __restrict__ S, const int32_t* __restrict__ index,
                                     const int32_t* __restrict__ n_dev, int64_t n, float delta,
+                                    float lower,
                                     int32_t* __restrict__ out, int32_t* __restrict__ count,
                                     int64_t capacity) {
   if (n_dev) {
@@ -24,7 +25,8 @@ __global__ void band_compact_kernel(const float* __restrict__ S, const int32_t* 
     int64_t p = 0;
     if (q < n) {
       p = index ? (int64_t)index[q] : q;
-      keep = fabsf(S[p]) < delta;
+      const float v = fabsf(S[p]);
+      keep = v < delta && v >= lower;
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     int b = 0;
@@ -53,7 +55,8 @@ extern "C" int mpl_band_compact(const float* S, const int32_t* index, const int3
   const int64_t cap = (int64_t)sm_count() * 8;
   if (blocks > cap) blocks = cap;
   band_compact_kernel<<<(unsigned)blocks, threads, 0, s>>>(S, index, n_dev, n, band->delta,
-                                                           band->out_index, band->count_dev,
+                                                           band->lower, band->out_index,
+                                                           band->count_dev,
                                                            band->capacity);
   MPL_LAUNCH_CHECK();
   return MPL_OK;

@@ -103,6 +103,7 @@ static int level_call(const MplNet* net, const void* packed, const MplPoints* po
     if (!band->out_index || !band->count_dev || band->capacity < 0) return MPL_ERR_INVALID_ARG;
     a.has_band = 1;
     a.band_delta = band->delta;
+    a.band_lower = band->lower;
     a.band_out = band->out_index;
     a.band_count = band->count_dev;
     a.band_capacity = band->capacity;
@@ -111,6 +112,7 @@ static int level_call(const MplNet* net, const void* packed, const MplPoints* po
   if (n == 0) return MPL_OK;
   if (precision == MPL_FP32) return launch_level_fp32(a, s);
   if (precision == MPL_BF16) return launch_level_bf16(a, s);
+  if (precision == MPL_F16) return launch_level_f16(a, s);
   return MPL_ERR_INVALID_ARG;
 }
 

@@ -177,6 +177,7 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 //         (LBO 128 B, SBO 256 B).  Multiplied by an A tile whose first two
 //         K columns are 1, one extra K=16 MMA step adds the bias exactly to
 //         ~16 bits.
+//   hwh_l, hbxh_l  hw_l and hbx_l with FP16 elements (the FP16 operand mode).
 struct PackLayout {
   int32_t L;    // nn.Linear layers
   int32_t WP;   // padded hidden width (64, 128 or 256)
@@ -186,6 +187,7 @@ struct PackLayout {
   int64_t w0f;
   int64_t hb[MPL_MAX_LAYERS];
   int64_t hw[MPL_MAX_LAYERS], hwT[MPL_MAX_LAYERS], hbx[MPL_MAX_LAYERS];
+  int64_t hwh[MPL_MAX_LAYERS], hbxh[MPL_MAX_LAYERS];  // the same two tiles in FP16
   int64_t total;
 };
 

@@ -17,6 +17,7 @@ struct LevelArgs {
   int32_t store_mode;
   int32_t has_band;
   float band_delta;
+  float band_lower;
   int32_t* band_out;
   int32_t* band_count;
   int64_t band_capacity;
@@ -58,7 +59,7 @@ __device__ __forceinline__ void store_and_band(const LevelArgs& a, bool valid, i
     a.S[p] = s;
   }
   if (a.has_band) {
-    const bool keep = valid && fabsf(s) < a.band_delta;
+    const bool keep = valid && fabsf(s) < a.band_delta && fabsf(s) >= a.band_lower;
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     const int lane = threadIdx.x & 31;
     int base = 0;
@@ -73,5 +74,6 @@ __device__ __forceinline__ void store_and_band(const LevelArgs& a, bool valid, i
 
 int launch_level_fp32(const LevelArgs& a, cudaStream_t s);
 int launch_level_bf16(const LevelArgs& a, cudaStream_t s);
+int launch_level_f16(const LevelArgs& a, cudaStream_t s);
 
 }  // namespace mpl

@@ -1,16 +1,24 @@
-// Dispatch of the BF16 tcgen05 level kernels (kernel template in
-// level_bf16.cuh): the epilogue unit width is a tuning option.
+// Dispatch of the tensor-core level kernels (kernel template in
+// level_bf16.cuh): operand type by precision (BF16 or FP16), epilogue unit
+// width by the MPL_OPT_BF16_EPILOGUE_UNIT option.
 #include "level.cuh"
 
 namespace mpl {
 
-int launch_level_bf16_u16(const LevelArgs& a, cudaStream_t s);
-int launch_level_bf16_u32(const LevelArgs& a, cudaStream_t s);
+int launch_level_tc_u16_bf16(const LevelArgs& a, cudaStream_t s);
+int launch_level_tc_u32_bf16(const LevelArgs& a, cudaStream_t s);
+int launch_level_tc_u16_f16(const LevelArgs& a, cudaStream_t s);
+int launch_level_tc_u32_f16(const LevelArgs& a, cudaStream_t s);
 
-int launch_level_bf16(const LevelArgs& a, cudaStream_t s) {
-  if (a.lay.nh == 0) return launch_level_fp32(a, s);  // no hidden GEMM to run in BF16
-  return option_value(MPL_OPT_BF16_EPILOGUE_UNIT) == 32 ? launch_level_bf16_u32(a, s)
-                                                        : launch_level_bf16_u16(a, s);
+int launch_level_tc(const LevelArgs& a, bool f16, cudaStream_t s) {
+  if (a.lay.nh == 0) return launch_level_fp32(a, s);  // no hidden GEMM for the tensor cores
+  const bool u32 = option_value(MPL_OPT_BF16_EPILOGUE_UNIT) == 32;
+  if (f16) return u32 ? launch_level_tc_u32_f16(a, s) : launch_level_tc_u16_f16(a, s);
+  return u32 ? launch_level_tc_u32_bf16(a, s) : launch_level_tc_u16_bf16(a, s);
 }
+
+int launch_level_bf16(const LevelArgs& a, cudaStream_t s) { return launch_level_tc(a, false, s); }
+
+int launch_level_f16(const LevelArgs& a, cudaStream_t s) { return launch_level_tc(a, true, s); }
 
 }  // namespace mpl

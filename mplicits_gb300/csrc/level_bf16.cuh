@@ -33,6 +33,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "level.cuh"
 #include "tc.cuh"
@@ -116,16 +117,35 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* s
 
 // A operand tile [128 x WP] bf16, K-major core matrices, layout
 // [k/8][m/8][m%8][k%8]: LBO (next 8 K) = 2048 B, SBO (next 8 rows) = 128 B.
-template <int U>
+// The two 16-bit operand types of kind::f16 (A and B always share one).
+template <typename T>
+struct Operand;
+template <>
+struct Operand<__nv_bfloat16> {
+  static constexpr uint32_t kFormat = 1;
+  __device__ static uint32_t pack(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+  }
+  __device__ static __nv_bfloat16 value(float f) { return __float2bfloat16_rn(f); }
+};
+template <>
+struct Operand<__half> {
+  static constexpr uint32_t kFormat = 0;
+  __device__ static uint32_t pack(float lo, float hi) {
+    __half2 v = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+  }
+  __device__ static __half value(float f) { return __float2half_rn(f); }
+};
+
+template <typename T, int U>
 __device__ __forceinline__ void store_a_unit(uint8_t* sA, int m, int j0, const float (&v)[U]) {
 #pragma unroll
   for (int g = 0; g < U / 8; ++g) {
     uint32_t w[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      __nv_bfloat162 b2 = __floats2bfloat162_rn(v[g * 8 + 2 * i], v[g * 8 + 2 * i + 1]);
-      w[i] = *reinterpret_cast<uint32_t*>(&b2);
-    }
+    for (int i = 0; i < 4; ++i) w[i] = Operand<T>::pack(v[g * 8 + 2 * i], v[g * 8 + 2 * i + 1]);
     const int k8 = (j0 >> 3) + g;
     const uint32_t off = (uint32_t)((k8 * 16 + (m >> 3)) * 128 + (m & 7) * 16);
     *reinterpret_cast<uint4*>(sA + off) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -135,7 +155,7 @@ __device__ __forceinline__ void store_a_unit(uint8_t* sA, int m, int j0, const f
 // Layer 0 of one U-feature unit (features j0..j0+U-1) for this thread's row:
 // FP32 phase omega0*(W0 x + b0) (omega folded into w0f), sine, BF16 into the
 // A operand.  GRAD: tangent row ch gets cos(z) * omega0*W0[:, ch-1].
-template <bool GRAD, int U>
+template <typename T, bool GRAD, int U>
 __device__ __forceinline__ void layer0_unit(uint8_t* sA, const float4* w0f, int m, int j0, int ch,
                                             float phase, float x, float y, float z) {
   float v[U];
@@ -151,10 +171,10 @@ __device__ __forceinline__ void layer0_unit(uint8_t* sA, const float4* w0f, int 
       v[jj] = sin_fast(zz);
     }
   }
-  store_a_unit<U>(sA, m, j0, v);
+  store_a_unit<T, U>(sA, m, j0, v);
 }
 
-template <int WP, bool GRAD, int STAGES, int U>
+template <int WP, bool GRAD, int STAGES, int U, typename T>
 __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const LevelArgs a) {
   using C = Bf16Cfg<WP, STAGES, U>;
   using E = Epi<U>;
@@ -166,7 +186,8 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
   constexpr int PT = GRAD ? kM / 4 : kM;  // points per tile
   constexpr int NC = C::NC;
   constexpr int S = C::kStages;
-  constexpr uint32_t IDESC = tc::idesc_bf16_f32(kM, WP);
+  constexpr uint32_t IDESC = tc::idesc_f16kind_f32(kM, WP, Operand<T>::kFormat);
+  constexpr bool kF16 = Operand<T>::kFormat == 0;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem + C::oA;
   uint8_t* sW = smem + C::oW;
@@ -220,7 +241,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
       wout[i] = reinterpret_cast<const float*>(pk + a.lay.wout)[i];
     }
     for (int l = 1; l <= nh; ++l) {
-      const uint4* gb = reinterpret_cast<const uint4*>(pk + a.lay.hbx[l]);
+      const uint4* gb = reinterpret_cast<const uint4*>(pk + (kF16 ? a.lay.hbxh[l] : a.lay.hbx[l]));
       uint4* db = reinterpret_cast<uint4*>(sBx + (l - 1) * C::kBxBytes);
       for (int i = threadIdx.x; i < (int)(C::kBxBytes / 16); i += kThreads) db[i] = gb[i];
     }
@@ -230,7 +251,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
       const int m = i >> 4, k = i & 15;
       const bool one = k < 2 && (!GRAD || (m & 3) == 0);
       const uint32_t off = (uint32_t)(((k >> 3) * 16 + (m >> 3)) * 128 + (m & 7) * 16 + (k & 7) * 2);
-      *reinterpret_cast<__nv_bfloat16*>(sAx + off) = __float2bfloat16_rn(one ? 1.f : 0.f);
+      *reinterpret_cast<T*>(sAx + off) = Operand<T>::value(one ? 1.f : 0.f);
     }
     fence_proxy_async_smem();
   }
@@ -246,7 +267,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
       int64_t w = 0;
       for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
         for (int l = 1; l <= nh && !*abort_flag; ++l) {
-          const char* src = pk + a.lay.hw[l];
+          const char* src = pk + (kF16 ? a.lay.hwh[l] : a.lay.hw[l]);
           for (int c = 0; c < NC; ++c, ++w) {
             const int s = (int)(w % S);
             const int64_t u = w / S;
@@ -340,7 +361,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
     }
 #pragma unroll 1
     for (int c = 0; c < NC; ++c) {
-      layer0_unit<GRAD, U>(sA, w0f, m, c * kKC + h * U, ch, phase, x, y, z);
+      layer0_unit<T, GRAD, U>(sA, w0f, m, c * kKC + h * U, ch, phase, x, y, z);
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&achunk[c]);
@@ -394,7 +415,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
 #pragma unroll
               for (int jj = 0; jj < U; ++jj)
                 v[jj] = GRAD ? __uint_as_float(r[jj]) : sin_fast(__uint_as_float(r[jj]));
-              store_a_unit<U>(sA, m, j0, v);
+              store_a_unit<T, U>(sA, m, j0, v);
               fence_proxy_async_smem();
               __syncwarp();
               if (lane == 0) mbar_arrive(&achunk[c]);
@@ -405,7 +426,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
                 part = __fmaf_rn(sv, wout[j0 + jj], part);
               }
               if (has_next) {
-                layer0_unit<GRAD, U>(sA, w0f, m, j0, ch, phase, xn, yn, zn);
+                layer0_unit<T, GRAD, U>(sA, w0f, m, j0, ch, phase, xn, yn, zn);
                 fence_proxy_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&achunk[c]);
@@ -462,12 +483,12 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
   if (warp == kMmaWarp) tc::tmem_dealloc(tmem, C::kTmemCols);
 }
 
-template <int WP, bool GRAD, int STAGES, int U>
+template <int WP, bool GRAD, int STAGES, int U, typename T>
 int launch_cfg(const LevelArgs& a, cudaStream_t s) {
   using C = Bf16Cfg<WP, STAGES, U>;
   constexpr int PT = GRAD ? kM / 4 : kM;
   const size_t smem = C::bytes(a.lay.nh);
-  MPL_CUDA_TRY(cudaFuncSetAttribute(level_bf16_kernel<WP, GRAD, STAGES, U>,
+  MPL_CUDA_TRY(cudaFuncSetAttribute(level_bf16_kernel<WP, GRAD, STAGES, U, T>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t grid = sm_count();
   if (!a.n_dev) {
@@ -475,29 +496,29 @@ int launch_cfg(const LevelArgs& a, cudaStream_t s) {
     grid = ntiles < grid ? ntiles : grid;
   }
   if (grid <= 0) return MPL_OK;
-  level_bf16_kernel<WP, GRAD, STAGES, U><<<(unsigned)grid, Epi<U>::kThreads, smem, s>>>(a);
+  level_bf16_kernel<WP, GRAD, STAGES, U, T><<<(unsigned)grid, Epi<U>::kThreads, smem, s>>>(a);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }
 
 // the deepest weight ring that fits the shared memory next to this level's
 // bias tiles
-template <int WP, bool GRAD, int U>
+template <int WP, bool GRAD, int U, typename T>
 int launch_wp(const LevelArgs& a, cudaStream_t s) {
   constexpr size_t kLimit = 227 * 1024;
   constexpr int SHI = WP == 256 ? 4 : 6;
-  if (Bf16Cfg<WP, SHI, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, GRAD, SHI, U>(a, s);
-  if (Bf16Cfg<WP, 3, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, GRAD, 3, U>(a, s);
-  if (Bf16Cfg<WP, 2, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, GRAD, 2, U>(a, s);
+  if (Bf16Cfg<WP, SHI, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, GRAD, SHI, U, T>(a, s);
+  if (Bf16Cfg<WP, 3, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, GRAD, 3, U, T>(a, s);
+  if (Bf16Cfg<WP, 2, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, GRAD, 2, U, T>(a, s);
   return MPL_ERR_UNSUPPORTED;
 }
 
-template <int U>
+template <int U, typename T>
 int launch_unit(const LevelArgs& a, cudaStream_t s) {
   switch (a.lay.WP) {
-    case 64: return a.grad ? launch_wp<64, true, U>(a, s) : launch_wp<64, false, U>(a, s);
-    case 128: return a.grad ? launch_wp<128, true, U>(a, s) : launch_wp<128, false, U>(a, s);
-    case 256: return a.grad ? launch_wp<256, true, U>(a, s) : launch_wp<256, false, U>(a, s);
+    case 64: return a.grad ? launch_wp<64, true, U, T>(a, s) : launch_wp<64, false, U, T>(a, s);
+    case 128: return a.grad ? launch_wp<128, true, U, T>(a, s) : launch_wp<128, false, U, T>(a, s);
+    case 256: return a.grad ? launch_wp<256, true, U, T>(a, s) : launch_wp<256, false, U, T>(a, s);
     default: return MPL_ERR_UNSUPPORTED;
   }
 }

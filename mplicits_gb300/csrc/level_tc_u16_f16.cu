@@ -1,0 +1,8 @@
+// Tensor-core level kernels: 16-feature epilogue units, F16 operands.
+#include "level_bf16.cuh"
+
+namespace mpl {
+int launch_level_tc_u16_f16(const LevelArgs& a, cudaStream_t s) {
+  return bf16::launch_unit<16, __half>(a, s);
+}
+}  // namespace mpl

@@ -1,0 +1,8 @@
+// Tensor-core level kernels: 32-feature epilogue units, BF16 operands.
+#include "level_bf16.cuh"
+
+namespace mpl {
+int launch_level_tc_u32_bf16(const LevelArgs& a, cudaStream_t s) {
+  return bf16::launch_unit<32, __nv_bfloat16>(a, s);
+}
+}  // namespace mpl

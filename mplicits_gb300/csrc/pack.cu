@@ -2,6 +2,7 @@
 // read.  Replaces the per-layer CUTLASS tensors of the reference renderer
 // (renderer/cuda/gemms.cu:5-100, loaded by tools.cu:81-111).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "common.cuh"
 
@@ -31,6 +32,7 @@ int make_layout(const MplNet* net, PackLayout* lay) {
   lay->b0 = take(WP * 4);
   for (int l = 0; l < MPL_MAX_LAYERS; ++l) {
     lay->wht[l] = lay->bh[l] = lay->hb[l] = lay->hw[l] = lay->hwT[l] = lay->hbx[l] = -1;
+    lay->hwh[l] = lay->hbxh[l] = -1;
   }
   for (int l = 1; l <= L - 2; ++l) {
     lay->wht[l] = take((int64_t)WP * WP * 4);
@@ -44,6 +46,8 @@ int make_layout(const MplNet* net, PackLayout* lay) {
     lay->hw[l] = take((int64_t)WP * WP * 2);
     lay->hwT[l] = take((int64_t)WP * WP * 2);
     lay->hbx[l] = take((int64_t)WP * 16 * 2);
+    lay->hwh[l] = take((int64_t)WP * WP * 2);
+    lay->hbxh[l] = take((int64_t)WP * 16 * 2);
   }
   lay->total = o;
   return MPL_OK;
@@ -72,7 +76,7 @@ __global__ void pack_layer0(const float* __restrict__ W, const float* __restrict
 
 __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict__ b, int out,
                             int in, int WP, float omega, float* wt, float* bh, float* hb,
-                            __nv_bfloat16* hw, __nv_bfloat16* hwT) {
+                            __nv_bfloat16* hw, __nv_bfloat16* hwT, __half* hwh) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)WP * WP) return;
   const int n = (int)(e / WP), k = (int)(e % WP);  // n: output row, k: input col
@@ -80,6 +84,7 @@ __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict
   wt[(int64_t)k * WP + n] = w;
   hw[umma_tile_offset(n, k, WP)] = __float2bfloat16_rn(omega * w);
   hwT[umma_tile_offset(k, n, WP)] = __float2bfloat16_rn(omega * w);
+  hwh[umma_tile_offset(n, k, WP)] = __float2half_rn(omega * w);
   if (k == 0) {
     const float bb = n < out ? b[n] : 0.f;
     bh[n] = bb;
@@ -89,17 +94,21 @@ __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict
 
 // bias tile of the MMA (see PackLayout::hbx): row n, K columns 0 and 1
 __global__ void pack_bias_tile(const float* __restrict__ b, int out, int WP, float omega,
-                               __nv_bfloat16* hbx) {
+                               __nv_bfloat16* hbx, __half* hbxh) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= WP) return;
   const float v = n < out ? omega * b[n] : 0.f;
-  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-  const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
   const int base = ((n >> 3) * 2) * 64 + (n & 7) * 8;  // elements; K group 0
-  for (int k = 0; k < 8; ++k) hbx[base + k] = __float2bfloat16_rn(0.f);
-  for (int k = 0; k < 8; ++k) hbx[base + 64 + k] = __float2bfloat16_rn(0.f);
+  for (int k = 0; k < 8; ++k) {
+    hbx[base + k] = hbx[base + 64 + k] = __float2bfloat16_rn(0.f);
+    hbxh[base + k] = hbxh[base + 64 + k] = __float2half_rn(0.f);
+  }
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
   hbx[base + 0] = hi;
-  hbx[base + 1] = lo;
+  hbx[base + 1] = __float2bfloat16_rn(v - __bfloat162float(hi));
+  const __half hh = __float2half_rn(v);
+  hbxh[base + 0] = hh;
+  hbxh[base + 1] = __float2half_rn(v - __half2float(hh));
 }
 
 __global__ void pack_output(const float* __restrict__ W, const float* __restrict__ b, int in,
@@ -147,11 +156,13 @@ extern "C" int mpl_net_pack(const MplNet* net, const float* const* weights,
     pack_hidden<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         weights[l], biases[l], net->dims[l + 1], net->dims[l], WP, net->omega[l],
         (float*)(base + lay.wht[l]), (float*)(base + lay.bh[l]), (float*)(base + lay.hb[l]),
-        (__nv_bfloat16*)(base + lay.hw[l]), (__nv_bfloat16*)(base + lay.hwT[l]));
+        (__nv_bfloat16*)(base + lay.hw[l]), (__nv_bfloat16*)(base + lay.hwT[l]),
+        (__half*)(base + lay.hwh[l]));
     MPL_LAUNCH_CHECK();
     pack_bias_tile<<<(WP + 127) / 128, 128, 0, s>>>(biases[l], net->dims[l + 1], WP,
                                                     net->omega[l],
-                                                    (__nv_bfloat16*)(base + lay.hbx[l]));
+                                                    (__nv_bfloat16*)(base + lay.hbx[l]),
+                                                    (__half*)(base + lay.hbxh[l]));
     MPL_LAUNCH_CHECK();
   }
   pack_output<<<(WP + 127) / 128, 128, 0, s>>>(weights[lay.L - 1], biases[lay.L - 1],

@@ -25,12 +25,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// Instruction descriptor of kind::f16: D f32, A and B bf16, both K-major.
-//   bits 4-5 D format (1: f32), 7-9 A format (1: bf16), 10-12 B format
-//   (1: bf16), 15/16 A/B major (0: K), 17-22 N >> 3, 24-28 M >> 4.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+// Instruction descriptor of kind::f16 with FP32 accumulation, A and B of the
+// same 16-bit type (fmt 1: bf16, 0: f16), both K-major:
+//   bits 4-5 D format (1: f32), 7-9 A format, 10-12 B format, 15/16 A/B
+//   major (0: K), 17-22 N >> 3, 24-28 M >> 4.
+__host__ __device__ constexpr uint32_t idesc_f16kind_f32(int M, int N, uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) |
          ((uint32_t)(M >> 4) << 24);
+}
+
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return idesc_f16kind_f32(M, N, 1u);
 }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {

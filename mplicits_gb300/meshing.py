@@ -94,9 +94,16 @@ class BandedReconstruction:
 
     ``levels`` are SIREN modules (coarse first); ``deltas`` one per residual
     level (empty: evaluate every level everywhere, i3d/meshing.py:232-233).
+
+    ``refine_margin`` (tensor-core precisions only): an upper bound m of the
+    tensor-core error of a partial sum.  Points whose value lies within m of
+    a band threshold are re-evaluated with the FP32 kernels before the band
+    list is cut, and points with |S| < m after the last level get every level
+    in FP32, so the band decisions and the marching-cubes signs are those of
+    the plain FP32 path.
     """
 
-    def __init__(self, levels, deltas, N, device="cuda", precision=None):
+    def __init__(self, levels, deltas, N, device="cuda", precision=None, refine_margin=None):
         self.levels = list(levels)
         self.deltas = list(deltas or [])
         self.N = int(N)
@@ -123,14 +130,81 @@ class BandedReconstruction:
                              count_dev=self.band_count[i:].data_ptr(), capacity=n)
             self._bands.append(b)
         self.mc = None
+        self.refine_margin = float(refine_margin) if refine_margin else 0.0
+        if self.refine_margin:
+            if self.deltas and self.refine_margin >= min(self.deltas[:m]):
+                raise ValueError("refine_margin must be smaller than every band width")
+            self.cand_index = [torch.empty(n, dtype=torch.int32, device=self.device)
+                               for _ in range(m)]
+            self.amb_index = torch.empty(n, dtype=torch.int32, device=self.device)
+            self.aux_count = torch.zeros(m + 1, dtype=torch.int32, device=self.device)
 
     def _prec(self, model):
         return capi.PRECISIONS[self.precision or getattr(model, "precision", "fp32")]
+
+    def _band(self, delta, out, count_view, lower=0.0):
+        return capi.MplBand(delta=float(delta), out_index=out.data_ptr(),
+                            count_dev=count_view.data_ptr(), capacity=self.n, lower=float(lower))
+
+    def _level(self, i, precision, mode, index=None, count=None, band=None, st=None):
+        net, packed = self.levels[i].packed()
+        capi.check(capi.load().mpl_level_forward(
+            ctypes.byref(net), capi.ptr(packed), ctypes.byref(self.points), capi.ptr(index),
+            capi.ptr(count), self.n, capi.ptr(self.S), mode,
+            None if band is None else ctypes.byref(band), precision, st), "mpl_level_forward")
+
+    def _compact(self, band, index, count, st):
+        capi.check(capi.load().mpl_band_compact(
+            capi.ptr(self.S), capi.ptr(index), capi.ptr(count), self.n, ctypes.byref(band), st),
+            "mpl_band_compact")
+
+    def _sample_refined(self, st):
+        """Tensor-core levels with FP32 re-evaluation inside the margins."""
+        m = self.refine_margin
+        fp32 = capi.MPL_FP32
+        amb, amb_n = self.amb_index, self.aux_count[len(self.cand_index):]
+        L = len(self.levels)
+        keep = []  # (band structs) kept alive until the launches are queued
+        idx, cnt = None, None
+        for i in range(L):
+            prec = self._prec(self.levels[i])
+            mode = capi.MPL_STORE if i == 0 else capi.MPL_ACCUMULATE
+            if i < len(self.cand_index):
+                cand, cand_n = self.cand_index[i], self.aux_count[i:]
+                b = self._band(self.deltas[i] + m, cand, cand_n)
+                keep.append(b)
+                self._level(i, prec, mode, idx, cnt, b, st)
+                # the ambiguous shell of this threshold, re-evaluated in FP32
+                ba = self._band(self.deltas[i] + m, amb, amb_n, lower=self.deltas[i] - m)
+                keep.append(ba)
+                self._compact(ba, cand, cand_n, st)
+                for k in range(i + 1):
+                    self._level(k, fp32, capi.MPL_STORE if k == 0 else capi.MPL_ACCUMULATE,
+                                amb, amb_n, None, st)
+                # the exact band list from the corrected values
+                self._compact(self._bands[i], cand, cand_n, st)
+                idx, cnt = self.band_index[i], self.band_count[i:]
+            else:
+                self._level(i, prec, mode, idx, cnt, None, st)
+        # the zero level: every level in FP32 where |S| < m
+        bz = self._band(m, amb, amb_n)
+        keep.append(bz)
+        if idx is None:
+            self._compact(bz, None, None, st)
+        else:
+            self._compact(bz, idx, cnt, st)
+        for k in range(L):
+            self._level(k, fp32, capi.MPL_STORE if k == 0 else capi.MPL_ACCUMULATE, amb, amb_n,
+                        None, st)
+        self._keep = keep
+        return self.S
 
     def sample(self, stream=None):
         """Evaluate S over the grid (stream-ordered, no host sync)."""
         lib = capi.load()
         st = capi.stream_ptr(stream)
+        if self.refine_margin and any(self._prec(mo) != capi.MPL_FP32 for mo in self.levels):
+            return self._sample_refined(st)
         for i, model in enumerate(self.levels):
             net, packed = model.packed()
             if i == 0:

@@ -19,17 +19,21 @@ def bf16_round(a):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def emulate_bf16_level(params, omegas, x):
+def f16_round(a):
+    return np.asarray(a, np.float32).astype(np.float16).astype(np.float64)
+
+
+def emulate_bf16_level(params, omegas, x, rnd=bf16_round):
     """The kernel's arithmetic in float64: FP32-phase layer 0 with omega
-    folded, BF16 activations and BF16 omega*W in the hidden GEMMs, FP32
-    sines into the output layer."""
+    folded, 16-bit activations and 16-bit omega*W in the hidden GEMMs (``rnd``
+    rounds to BF16 or FP16), FP32 sines into the output layer."""
     W0, b0 = params[0]
     z = np.asarray(x, np.float64) @ (omegas[0] * W0.astype(np.float64)).T + omegas[0] * b0
     s = np.sin(z)
     for l in range(1, len(params) - 1):
         W, b = params[l]
-        Wq = bf16_round(np.float32(omegas[l]) * W.astype(np.float32))
-        z = bf16_round(s.astype(np.float32)) @ Wq.T + omegas[l] * b.astype(np.float64)
+        Wq = rnd(np.float32(omegas[l]) * W.astype(np.float32))
+        z = rnd(s.astype(np.float32)) @ Wq.T + omegas[l] * b.astype(np.float64)
         s = np.sin(z)
     Wl, bl = params[-1]
     return (s @ Wl.astype(np.float64).T + bl)[:, 0]
@@ -52,16 +56,17 @@ def epilogue_unit(request, lib):
     capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
 
 
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
 @pytest.mark.parametrize("cfg", [[256, 256, 256], [128, 128, 128], [64, 64], [100, 60, 17],
                                  [256, 256, 256, 256, 256]])
 @pytest.mark.parametrize("P", [1, 200, 20000])
-def test_bf16_tensor_core_arithmetic_is_exact(lib, epilogue_unit, cfg, P):
+def test_bf16_tensor_core_arithmetic_is_exact(lib, epilogue_unit, cfg, P, prec):
     from mplicits_gb300.model import level_forward
     m, params = _model(cfg, 7 + len(cfg))
     rng = np.random.default_rng(P)
     x = rng.uniform(-1, 1, (P, 3)).astype(np.float32)
-    out = level_forward(m, torch.from_numpy(x).cuda(), precision="bf16").cpu().numpy()
-    emu = emulate_bf16_level(params, m.omegas(), x)
+    out = level_forward(m, torch.from_numpy(x).cuda(), precision=prec).cpu().numpy()
+    emu = emulate_bf16_level(params, m.omegas(), x, bf16_round if prec == "bf16" else f16_round)
     # exact up to accumulation order and the hardware sine (~1e-6 for these
     # phases); a BF16 rounding flip of an activation moves a rare point by up
     # to ~1e-3.  A wrong descriptor or tile layout gives O(1) errors.
@@ -101,3 +106,21 @@ def test_bf16_grid_band_pipeline_matches_fp32_bands_where_clear(lib):
     b16 = set(rec16.band_index[0][:k16].cpu().tolist())
     diff = b32 ^ b16
     assert all(abs(abs(S0[p]) - 0.05) < 5e-3 for p in diff)
+
+
+def test_fp16_operands_meet_the_error_target_on_trained_levels(lib):
+    """The trained three-level fixture: FP16 operands keep every level within
+    5e-4 of the FP64 oracle (BF16 does not in the far field)."""
+    from mplicits_gb300.model import SIREN, level_forward
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "three_level_sphere.npz"))
+    x = np.random.default_rng(4).uniform(-1, 1, (1 << 17, 3)).astype(np.float32)
+    for i in range(3):
+        sd = {k[3:]: d[k] for k in d.files if k.startswith(f"L{i}.")}
+        m = SIREN(3, 1, [256, 256, 256], w0=30, delay_init=True, precision="fp16")
+        m.load_state_dict({k: torch.from_numpy(v) for k, v in sd.items()})
+        m = m.cuda().eval()
+        params = siren.params_from_state_dict({k: v.cpu().numpy() for k, v in m.state_dict().items()})
+        out = level_forward(m, torch.from_numpy(x).cuda()).cpu().numpy()
+        ref = siren.siren_forward(params, m.omegas(), x, np.float64)
+        assert np.abs(out - ref).max() <= 5e-4, i

@@ -68,3 +68,42 @@ def test_create_mesh_multistage_drop_in(lib, tmp_path):
     with open(path, "rb") as fh:
         head = fh.read(200)
     assert head.startswith(b"ply\nformat binary_little_endian 1.0\nelement vertex ")
+
+
+def _trained_levels(precision):
+    from mplicits_gb300.model import SIREN
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "three_level_sphere.npz"))
+    out = []
+    for i in range(3):
+        sd = {k[3:]: d[k] for k in d.files if k.startswith(f"L{i}.")}
+        m = SIREN(3, 1, [256, 256, 256], w0=30, delay_init=True, precision=precision)
+        m.load_state_dict({k: torch.from_numpy(v) for k, v in sd.items()})
+        out.append(m.cuda().eval())
+    return out
+
+
+@pytest.mark.parametrize("precision,margin", [("bf16", 2e-3), ("fp16", 1e-3)])
+def test_refined_tensor_core_bands_and_mesh_topology_equal_fp32(lib, precision, margin):
+    """With the FP32 re-evaluation margin, the tensor-core pipeline cuts the
+    same band lists as the plain FP32 pipeline and its marching cubes sees the
+    same signs (identical face arrays) on the trained three-level model."""
+    from mplicits_gb300.meshing import BandedReconstruction
+    N, deltas = 128, [0.05, 0.01]
+    ref = BandedReconstruction(_trained_levels("fp32"), deltas, N, "cuda")
+    ref.sample()
+    rec = BandedReconstruction(_trained_levels(precision), deltas, N, "cuda", precision,
+                               refine_margin=margin)
+    rec.sample()
+    for i in range(2):
+        a = np.sort(ref.band_index[i][:ref.band_sizes()[i]].cpu().numpy())
+        b = np.sort(rec.band_index[i][:rec.band_sizes()[i]].cpu().numpy())
+        assert np.array_equal(a, b), i
+    va, fa, _, _ = ref.mesh()
+    vb, fb, _, _ = rec.mesh()
+    assert torch.equal(fa, fb)
+    # vertices with an end within the margin are FP32; the rest carry the
+    # tensor-core error only
+    assert (va - vb).abs().max().item() < 2.0 / (N - 1)
+    S32, S16 = ref.S.cpu().numpy(), rec.S.cpu().numpy()
+    near = np.abs(S16) < margin  # the points the zero-level pass recomputed in FP32
+    assert near.any() and np.array_equal(S32[near], S16[near])
