@@ -230,6 +230,46 @@ int mpl_trace_shade(const float* origins_dev, const float* dirs_dev, const float
                     const int32_t* state_dev, int64_t P, int32_t mode, uint32_t* image_dev,
                     void* stream);
 
+/* ---- training (i3d/loss_functions.py:327-394,
+ *      experiment_scripts/train_sdf_on_neighborhood_fine.py:197-262) ------- */
+
+/* Floats of the pre-activation scratch of mpl_train_forward for n points:
+ * (hidden GEMMs + 1) * n * 4 * padded width. */
+int mpl_train_scratch_floats(const MplNet* net, int64_t n, int64_t* floats);
+
+/* Plain-form forward of a trainable level on xyz [n, 3]: S [n], G [n, 3]
+ * (df/dx) and the pre-activations of every layer for the backward. */
+int mpl_train_forward(const MplNet* net, const void* packed_dev, const float* xyz_dev, int64_t n,
+                      float* S_dev, float* G_dev, float* pre_dev, void* stream);
+
+/* The residual-level loss of the reference's fine trainer on n points
+ * (loss_add_detail_fine): with S = f + f_frozen and G = g + g_frozen,
+ * sdf (gt - S)^2 and normal 1 - cos(n_gt, G) where gt_sdf != -1, eikonal
+ * (|G| - 1)^2 everywhere.  Writes the three sums to loss_sums[3] (divide by
+ * n and weight as the reference does) and the derivative seeds
+ * seeds [n, 4] = (dL/df, dL/dG) of the weighted mean loss.  f_frozen and
+ * g_frozen are nullable (no frozen levels). */
+int mpl_train_loss(int64_t n, const float* f_dev, const float* g_dev, const float* f_frozen_dev,
+                   const float* g_frozen_dev, const float* gt_sdf_dev, const float* gt_normals_dev,
+                   float w_sdf, float w_normal, float w_eikonal, float* seeds_dev,
+                   float* loss_sums_dev, void* stream);
+
+/* Weight gradients of a loss given its seeds on (f, df/dx) of every point:
+ * the backward through the level's forward-mode graph (double backward of
+ * the input gradient included).  dW[l] / db[l] are device buffers of the
+ * padded shapes ([WP][3] for layer 0, [WP][WP] hidden, [WP] output; bias
+ * [WP], output bias [1]); the call ADDS into them.  `da` is scratch of the
+ * same size as the pre-activations.  Replaces autograd's backward of
+ * torch.autograd.grad(..., create_graph=True) in the reference trainers. */
+int mpl_train_backward(const MplNet* net, const void* packed_dev, const float* xyz_dev, int64_t n,
+                       const float* pre_dev, const float* seeds_dev, float* da_dev,
+                       float* const* dW_dev, float* const* db_dev, void* stream);
+
+/* One torch.optim.Adam step (no weight decay) over `count` FP32 tensors. */
+int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* grads_dev,
+                  float* const* exp_avg_dev, float* const* exp_avg_sq_dev, const int64_t* numel,
+                  float lr, float beta1, float beta2, float eps, int64_t step, void* stream);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* Process-wide kernel options (read at each launch). */

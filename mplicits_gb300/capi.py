@@ -91,6 +91,13 @@ SIGNATURES = {
     "mpl_trace_step": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _F, _F, _I32, _P, _P, _P, _P,
                                       _I64, _P]),
     "mpl_trace_shade": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P]),
+    "mpl_train_scratch_floats": (ctypes.c_int, [ctypes.POINTER(MplNet), _I64,
+                                                ctypes.POINTER(_I64)]),
+    "mpl_train_forward": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _P, _I64, _P, _P, _P, _P]),
+    "mpl_train_loss": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P, _P, _F, _F, _F, _P, _P, _P]),
+    "mpl_train_backward": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _P, _I64, _P, _P, _P, _P,
+                                          _P, _P]),
+    "mpl_adam_step": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _F, _F, _F, _F, _I64, _P]),
     "mpl_set_option": (ctypes.c_int, [_I32, _I64]),
     "mpl_get_option": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
     "mpl_status_string": (ctypes.c_char_p, [ctypes.c_int]),

@@ -178,6 +178,8 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 //         K columns are 1, one extra K=16 MMA step adds the bias exactly to
 //         ~16 bits.
 //   hwh_l, hbxh_l  hw_l and hbx_l with FP16 elements (the FP16 operand mode).
+//   whn_l [WP][WP] FP32 W_l untransposed (j, k): the B operand of the
+//         backward GEMM d_in = d_a W_l.
 struct PackLayout {
   int32_t L;    // nn.Linear layers
   int32_t WP;   // padded hidden width (64, 128 or 256)
@@ -188,6 +190,7 @@ struct PackLayout {
   int64_t hb[MPL_MAX_LAYERS];
   int64_t hw[MPL_MAX_LAYERS], hwT[MPL_MAX_LAYERS], hbx[MPL_MAX_LAYERS];
   int64_t hwh[MPL_MAX_LAYERS], hbxh[MPL_MAX_LAYERS];  // the same two tiles in FP16
+  int64_t whn[MPL_MAX_LAYERS];  // FP32 W_l as stored by nn.Linear, [j][k] (backward GEMM)
   int64_t total;
 };
 

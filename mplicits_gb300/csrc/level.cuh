@@ -24,6 +24,10 @@ struct LevelArgs {
   int* status;  // device status word
   int32_t grad;  // also compute df/dx (forward mode) into G
   float* G;      // [*, 3] gradients, indexed like S (nullable in grad mode)
+  // training: pre-activations a_l of every layer and row, FP32 plain GRAD
+  // kernel only: pre[((l * n + q) * 4 + row) * WP + j] (row 0 value with bias,
+  // rows 1..3 the tangents d/dx, d/dy, d/dz without bias)
+  float* pre;
 };
 
 __device__ __forceinline__ int64_t level_point_count(const LevelArgs& a) {

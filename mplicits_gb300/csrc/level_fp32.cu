@@ -180,6 +180,28 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
       // ---- epilogue of this layer: s = sin(omega * (acc + b))
       const float om = a.omega[layer];
       const float* bias = layer == 0 ? b0 : bh + (layer - 1) * WP;
+      if (GRAD && a.pre) {
+        // training: keep the pre-activations of every row for the backward
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int row = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+          const int64_t qq = t * PT + (row >> 2);
+          if (qq < n) {
+            float* dst = a.pre + (((int64_t)layer * n + qq) * 4 + (i & 3)) * WP;
+#pragma unroll
+            for (int f4 = 0; f4 < FPT / 4; ++f4) {
+              const int j = tx * 4 + 64 * f4;
+              float4 v;
+              const bool val = (i & 3) == 0;
+              v.x = val ? __fadd_rn(acc[i][4 * f4 + 0], bias[j + 0]) : acc[i][4 * f4 + 0];
+              v.y = val ? __fadd_rn(acc[i][4 * f4 + 1], bias[j + 1]) : acc[i][4 * f4 + 1];
+              v.z = val ? __fadd_rn(acc[i][4 * f4 + 2], bias[j + 2]) : acc[i][4 * f4 + 2];
+              v.w = val ? __fadd_rn(acc[i][4 * f4 + 3], bias[j + 3]) : acc[i][4 * f4 + 3];
+              *reinterpret_cast<float4*>(dst + j) = v;
+            }
+          }
+        }
+      }
       if (layer < nh) {
         float4* actw = reinterpret_cast<float4*>(act);
 #pragma unroll

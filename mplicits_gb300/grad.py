@@ -43,22 +43,26 @@ def level_gradient(model, x, S=None, G=None, accumulate=False, precision=None, i
 def level_backward(model, x, gy, params, needs_input_grad):
     """Backward of model_out = f(x) for ``_LevelForward``.
 
-    d(model_in) = gy * df/dx comes from the fused gradient kernel.  Weight
-    gradients and the double backward go through ``mplicits_gb300.train``
-    (the training step); plain autograd into the parameters is refused
-    rather than silently returning zeros.
+    d(model_in) = gy * df/dx comes from the fused gradient kernel; under
+    ``create_graph=True`` (i3d/diff_operators.py:259-265) it is the
+    differentiable op of ``mplicits_gb300.train.level_input_grad``, whose own
+    backward is the double backward of the eikonal and normal losses.
+    Weight gradients come from the hand-written backward kernels
+    (``mplicits_gb300.train.param_grads``) with seed gy.
     """
-    if any(needs_input_grad[2:]):
-        raise NotImplementedError(
-            "weight gradients of mplicits_gb300.SIREN are produced by the fused training "
-            "step (mplicits_gb300.train); wrap inference in torch.no_grad() or set "
-            "requires_grad_(False) on the parameters")
-    if torch.is_grad_enabled():
-        raise NotImplementedError(
-            "create_graph=True through mplicits_gb300.SIREN needs the training step "
-            "(mplicits_gb300.train), which differentiates the gradient analytically")
+    from . import train as _train
+    shape = x.shape
+    x2 = x.detach().reshape(-1, shape[-1])
+    g2 = gy.reshape(-1)
     dx = None
     if needs_input_grad[0]:
-        _, G = level_gradient(model, x)
-        dx = gy.reshape(-1, 1).to(G.dtype) * G
-    return (dx, None) + (None,) * len(params)
+        if torch.is_grad_enabled():
+            G = _train.level_input_grad(model, x.reshape(-1, shape[-1]))
+            dx = (gy.reshape(-1, 1) * G).reshape(shape)
+        else:
+            _, G = level_gradient(model, x2, precision="fp32")
+            dx = (g2.reshape(-1, 1).to(G.dtype) * G).reshape(shape)
+    pgrads = (None,) * len(params)
+    if any(needs_input_grad[2:]):
+        pgrads = tuple(_train.param_grads(model, x2, df=g2.detach()))
+    return (dx, None) + pgrads

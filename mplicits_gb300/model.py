@@ -99,10 +99,10 @@ class _LevelForward(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, x, model, *params):
-        out = level_forward(model, x)
+        out = level_forward(model, x.reshape(-1, x.shape[-1]))
         ctx.model = model
         ctx.save_for_backward(x, *params)
-        return out.unsqueeze(-1)
+        return out.reshape(x.shape[:-1] + (1,))
 
     @staticmethod
     def backward(ctx, gy):
@@ -194,7 +194,8 @@ class SIREN(nn.Module):
                                         any(p.requires_grad for p in params)):
             y = _LevelForward.apply(coords_org, self, *params)
         else:
-            y = level_forward(self, coords_org).unsqueeze(-1)
+            y = level_forward(self, coords_org.reshape(-1, coords_org.shape[-1]))
+            y = y.reshape(coords_org.shape[:-1] + (1,))
         return {"model_in": coords_org, "model_out": y}
 
     def reset_weights(self):
