@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--bf16-unit", type=int, default=None, choices=[16, 32],
                     help="epilogue unit width of the BF16 kernel (default: the library's)")
+    ap.add_argument("--skip-train", action="store_true")
+    ap.add_argument("--skip-trace", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="time only the BF16 steps (for profiler runs) and print a short line")
     return ap.parse_args()
@@ -361,6 +363,128 @@ def cpu_baseline(levels_np, N, slabs, threads, gpu_S=None):
     return N ** 3 / full, detail
 
 
+TRAIN_SURFACE = 1 << 16  # surface samples per batch; rows = 3x (surface, offset, dithered)
+# per row: two frozen levels and the trainable level in forward mode (value
+# row 2*(3*256 + 2*256*256 + 256), three tangent rows 2*(2*256*256 + 256)),
+# then the backward GEMM d_a W and the weight-gradient GEMM of the two hidden
+# layers over the four rows
+_FWD_TANGENT = 2 * (3 * 256 + 2 * 256 * 256 + 256) + 3 * 2 * (2 * 256 * 256 + 256)
+TRAIN_FLOP_PER_ROW = 3 * _FWD_TANGENT + 2 * (2 * 4 * 2 * 256 * 256)
+TRAIN_LAUNCHES_PER_STEP = 10  # batch, 2 frozen gradients, forward, loss, backward (4), Adam
+
+
+def train_surface(n=1 << 18, seed=1):
+    from mplicits_gb300.synthetic import surface_points
+    pts, nrm = surface_points(n, np.random.default_rng(seed), noise=0.002)
+    return np.concatenate([pts, nrm], 1).astype(np.float32)
+
+
+def train_bench(levels_np, device, K, W):
+    """The fine-level training step: batch construction on the device, the
+    frozen coarse and medium levels' f and df/dx, the trainable level's
+    forward, loss, hand-written backward and Adam."""
+    import torch
+    from mplicits_gb300.train import ResidualTrainer, create_training_data_on_neighborhood
+    V = torch.from_numpy(train_surface()).to(device)
+    models = make_models(levels_np, "fp32", device)
+    tr = ResidualTrainer(models[2], models[:2], lr=1e-4)
+    it = [0]
+
+    def step():
+        it[0] += 1
+        b = create_training_data_on_neighborhood(V, TRAIN_SURFACE, device=device, delta=0.01,
+                                                 seed=it[0])["on_surf"]
+        return tr.step(*b)
+
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        losses = step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    rows = 3 * TRAIN_SURFACE
+    return {"workload": f"fine-level residual training step: {TRAIN_SURFACE} surface samples "
+                        f"-> {rows} rows (surface, normal offset, delta1-dithered), level "
+                        "3->256x3->1 trainable, coarse and medium frozen, losses of "
+                        "loss_add_detail_fine, Adam lr 1e-4, FP32",
+            "value": rows / (ms * 1e-3), "unit": "rows/s", "ms_per_step": ms, "steps": K,
+            "warmup": W, "dtype": "f32", "flop_per_row": TRAIN_FLOP_PER_ROW,
+            "achieved_tflops": TRAIN_FLOP_PER_ROW * rows / (ms * 1e-3) / 1e12,
+            "last_losses": [float(x) for x in losses.cpu()],
+            "gpu_launches": K * TRAIN_LAUNCHES_PER_STEP}
+
+
+def train_cpu_baseline(levels_np, rows=3072, steps=3):
+    """The reference's training step as it runs on the CPU (torch autograd,
+    all host threads) on a bounded batch of the same kind of rows."""
+    import torch
+    from oracle.torch_ref import PlainSiren, train_step
+    from oracle import train as otrain
+    torch.set_num_threads(os.cpu_count() or 1)
+    om = [30.0, 30.0, 30.0]
+    fine = PlainSiren(levels_np[2][1], om)
+    frozen = [PlainSiren(levels_np[i][1], om) for i in range(2)]
+    for m in frozen:
+        m.requires_grad_(False)
+    opt = torch.optim.Adam(fine.parameters(), lr=1e-4)
+    verts = train_surface()
+    rng = np.random.default_rng(3)
+    n = rows // 3
+    idx = rng.choice(verts.shape[0], n, replace=False)
+    u = rng.random((n, 3)).astype(np.float32)
+    p, nr, s = [torch.from_numpy(a) for a in otrain.training_batch(verts, idx, u, 0.01)]
+    train_step(fine, frozen, opt, p, nr, s)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        train_step(fine, frozen, opt, p, nr, s)
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": rows / dt, "unit": "rows/s", "cores": torch.get_num_threads(),
+            "kind": "port", "sample": f"{steps} steps of {rows} rows with torch autograd on "
+                                      "the CPU (the reference's step restated)"}
+
+
+def trace_bench(levels_np, device, K, W, precision="bf16"):
+    """Sphere tracing of 1920x1080 frames from 8 orbit viewpoints."""
+    import torch
+    from mplicits_gb300.trace import SphereTracer, orbit_cameras
+    cams = orbit_cameras()
+    models = make_models(levels_np, precision, device)
+    tr = SphereTracer(models, DELTAS, 1920, 1080, max_steps=96, eps=1e-4, precision=precision)
+    for k in range(max(W, 1)):
+        tr.render(cams[k % len(cams)])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    hits = []
+    e0.record()
+    for k in range(K):
+        _, state = tr.render(cams[k % len(cams)])
+        hits.append(tr.counts[2:3].clone())
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    P = 1920 * 1080
+    return {"value": P / (ms * 1e-3), "unit": "rays/s", "ms_per_frame": ms, "frames": K,
+            "hits_per_frame": [int(h) for h in torch.cat(hits).cpu()],
+            "launches_per_frame": tr.launches_per_frame, "dtype": precision}, tr
+
+
+def trace_cpu_baseline(levels_np, W=192, H=108):
+    from oracle import trace as otrace
+    from mplicits_gb300.trace import orbit_cameras
+    cam = dict(orbit_cameras()[0])
+    cam["width"], cam["height"] = W, H
+    params = [(p, [30.0, 30.0, 30.0]) for _, p in levels_np]
+    t0 = time.perf_counter()
+    otrace.trace(params, DELTAS, cam, max_steps=96, eps=1e-4)
+    dt = time.perf_counter() - t0
+    return {"value": W * H / dt, "unit": "rays/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"one {W}x{H} frame of the first orbit camera, float64 numpy oracle"}
+
+
 def run_reference(args):
     rank, world, _ = rank_info()
     if rank != 0:
@@ -458,6 +582,24 @@ def main():
     # ---- end to end through the public API with host buffers
     e2e_s, h2d, d2h, e2e_launch = e2e_run(levels_np, N, device, max(1, K // 2), 1)
 
+    # ---- the training step and the sphere tracer
+    training = tracing = None
+    if not args.skip_train:
+        training = train_bench(levels_np, device, K, W)
+        if rank == 0 and not args.skip_cpu:
+            training["cpu_baseline"] = train_cpu_baseline(levels_np)
+    if not args.skip_trace:
+        tracing = {}
+        for prec in ("bf16", "fp32"):
+            tracing[prec], tr = trace_bench(levels_np, device, K if prec == "bf16" else 1, 1,
+                                            prec)
+            del tr
+        tracing["workload"] = ("1920x1080 pinhole rays, 45 deg, 8 orbit viewpoints at radius "
+                               "2.5, <= 96 steps, eps 1e-4, band-gated levels, gradient normals "
+                               "and shading of the hits")
+        if rank == 0 and not args.skip_cpu:
+            tracing["cpu_baseline"] = trace_cpu_baseline(levels_np)
+
     # ---- roofline of the dominant kernel (level 0 over the full grid)
     peak_tf, hbm, src = peaks()
     achieved_tf = FLOP_PER_POINT * N ** 3 / (l0_ms * 1e-3) / 1e12
@@ -504,6 +646,8 @@ def main():
                          "flop_per_point": FLOP_PER_POINT, "points_per_launch": N ** 3,
                          "launch_ms": l0_ms, "traffic": traffic},
             "cpu_baseline": cpu,
+            "training": training,
+            "sphere_tracing": tracing,
             "gpu_launches": K * KERNEL_LAUNCHES_PER_STEP,
             "clocks": clk.summary(),
         }

@@ -265,6 +265,27 @@ int mpl_train_backward(const MplNet* net, const void* packed_dev, const float* x
                        const float* pre_dev, const float* seeds_dev, float* da_dev,
                        float* const* dW_dev, float* const* db_dev, void* stream);
 
+/* Flags of mpl_train_batch. */
+#define MPL_BATCH_NEIGH_DELTA 1 /* offset scale from the last column (use_neigh_delta) */
+#define MPL_BATCH_DITHER 2      /* append the dithered rows (dithering_sampling)      */
+
+/* The residual trainers' batch, create_training_data_on_neighborhood
+ * (experiment_scripts/utils.py:92-169): from n of the n_vertices rows of
+ * `vertices` (row_floats >= 6 floats each: xyz, normal, [neighbourhood
+ * delta]) it writes n surface rows (sdf 0), n rows offset along the normal
+ * by d * u_z (sdf d * u_z, d = the row's delta or delta_eps) and, with
+ * MPL_BATCH_DITHER, n rows at x + delta * u + delta / 2 * normal (sdf -1):
+ * pts [2n or 3n, 3], normals [same, 3], sdf [same].  sample_index [n] (the
+ * reference's randperm prefix) and uniforms [n, 3] (its torch.rand draw) are
+ * nullable; when null they come from a counter-based generator keyed by
+ * `seed`, indices then drawn with replacement.  n <= n_vertices.  An index
+ * outside [0, n_vertices) zeroes its rows and sets MPL_ERR_INVALID_ARG in the
+ * device status word. */
+int mpl_train_batch(const float* vertices_dev, int64_t n_vertices, int32_t row_floats,
+                    const int64_t* sample_index_dev, const float* uniforms_dev, int64_t n,
+                    float delta, float delta_eps, int32_t flags, uint64_t seed, float* pts_dev,
+                    float* normals_dev, float* sdf_dev, void* stream);
+
 /* One torch.optim.Adam step (no weight decay) over `count` FP32 tensors. */
 int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* grads_dev,
                   float* const* exp_avg_dev, float* const* exp_avg_sq_dev, const int64_t* numel,

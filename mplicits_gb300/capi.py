@@ -33,6 +33,8 @@ MPL_POINTS_GRID = 1
 
 PRECISIONS = {"fp32": MPL_FP32, "bf16": MPL_BF16, "fp16": MPL_F16}
 MPL_OPT_BF16_EPILOGUE_UNIT = 1
+MPL_BATCH_NEIGH_DELTA = 1
+MPL_BATCH_DITHER = 2
 
 
 class MplNet(ctypes.Structure):
@@ -97,6 +99,8 @@ SIGNATURES = {
     "mpl_train_loss": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P, _P, _F, _F, _F, _P, _P, _P]),
     "mpl_train_backward": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _P, _I64, _P, _P, _P, _P,
                                           _P, _P]),
+    "mpl_train_batch": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _F, _F, _I32,
+                                       ctypes.c_uint64, _P, _P, _P, _P]),
     "mpl_adam_step": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _F, _F, _F, _F, _I64, _P]),
     "mpl_set_option": (ctypes.c_int, [_I32, _I64]),
     "mpl_get_option": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),

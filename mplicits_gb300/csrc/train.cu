@@ -385,6 +385,71 @@ __global__ void adam_kernel(const AdamArgs a) {
   }
 }
 
+// Counter-based random numbers for batches drawn on the device: SplitMix64
+// (Steele, Lea and Flood, "Fast splittable pseudorandom number generators",
+// OOPSLA 2014) applied to seed + index.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// create_training_data_on_neighborhood (experiment_scripts/utils.py:92-169)
+// for sample i: surface row i, the normal offset row n + i and, with
+// dithering, row 2n + i, each with the reference's float32 operation order.
+__global__ void train_batch_kernel(const float* __restrict__ V, int64_t M, int C,
+                                   const int64_t* __restrict__ idx, const float* __restrict__ u,
+                                   int64_t n, float delta, float half_delta, float delta_eps,
+                                   int neigh, int dither, uint64_t seed, float* __restrict__ pts,
+                                   float* __restrict__ nrm, float* __restrict__ sdf, int* status) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r;
+    if (idx) {
+      r = idx[i];
+    } else {
+      r = (int64_t)((splitmix64(seed * 0x100000001b3ull + (uint64_t)i) >> 11) % (uint64_t)M);
+    }
+    float x[3] = {0.f, 0.f, 0.f}, nm[3] = {0.f, 0.f, 0.f}, dn = delta_eps, uu[3];
+    if (r >= 0 && r < M) {
+      const float* v = V + r * C;
+      for (int c = 0; c < 3; ++c) {
+        x[c] = v[c];
+        nm[c] = v[3 + c];
+      }
+      if (neigh) dn = v[C - 1];
+    } else {
+      report_device_error(status, MPL_ERR_INVALID_ARG);
+    }
+    for (int c = 0; c < 3; ++c) {
+      if (u) {
+        uu[c] = u[3 * i + c];
+      } else {
+        const uint64_t h = splitmix64((seed ^ 0x5bd1e9955bd1e995ull) + 3ull * (uint64_t)i + c);
+        uu[c] = (float)(h >> 40) * 0x1p-24f;
+      }
+    }
+    const float s = __fmul_rn(dn, uu[2]);
+    for (int c = 0; c < 3; ++c) {
+      pts[3 * i + c] = x[c];
+      pts[3 * (n + i) + c] = __fadd_rn(x[c], __fmul_rn(s, nm[c]));
+      nrm[3 * i + c] = nm[c];
+      nrm[3 * (n + i) + c] = nm[c];
+    }
+    sdf[i] = 0.f;
+    sdf[n + i] = s;
+    if (dither) {
+      for (int c = 0; c < 3; ++c) {
+        pts[3 * (2 * n + i) + c] =
+            __fadd_rn(__fmul_rn(uu[c], delta), __fadd_rn(x[c], __fmul_rn(half_delta, nm[c])));
+        nrm[3 * (2 * n + i) + c] = nm[c];
+      }
+      sdf[2 * n + i] = -1.f;
+    }
+  }
+}
+
 template <int WP>
 int launch_backward_wp(const TrainArgs& t, cudaStream_t s) {
   const size_t smem = (size_t)WP * kRows * 4 + 2ull * kKC * WP * 4 + WP * 4 + 16;
@@ -488,6 +553,24 @@ extern "C" int mpl_train_backward(const MplNet* net, const void* packed, const f
   }
   dim3 g2((WP + 127) / 128, splits < 1 ? 1 : splits);
   train_wgrad_ends_kernel<<<g2, 128, 0, s>>>(t, WP, dW[0], db[0], dW[L - 1], db[L - 1]);
+  MPL_LAUNCH_CHECK();
+  return MPL_OK;
+}
+
+extern "C" int mpl_train_batch(const float* vertices, int64_t n_vertices, int32_t row_floats,
+                               const int64_t* sample_index, const float* uniforms, int64_t n,
+                               float delta, float delta_eps, int32_t flags, uint64_t seed,
+                               float* pts, float* normals, float* sdf, void* stream) {
+  if (!vertices || !pts || !normals || !sdf || n < 0 || n > n_vertices || row_floats < 6 ||
+      (flags & ~(MPL_BATCH_NEIGH_DELTA | MPL_BATCH_DITHER)))
+    return MPL_ERR_INVALID_ARG;
+  if ((flags & MPL_BATCH_NEIGH_DELTA) && row_floats < 7) return MPL_ERR_INVALID_ARG;
+  if (n == 0) return MPL_OK;
+  const int64_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  train_batch_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+      vertices, n_vertices, row_floats, sample_index, uniforms, n, delta,
+      (float)(0.5 * (double)delta), delta_eps, (flags & MPL_BATCH_NEIGH_DELTA) != 0,
+      (flags & MPL_BATCH_DITHER) != 0, seed, pts, normals, sdf, device_status_ptr());
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }

@@ -160,6 +160,45 @@ def level_input_grad(model, x):
     return _LevelInputGrad.apply(x, model, *model.parameters())
 
 
+def create_training_data_on_neighborhood(vertices, n_on_surf, device="cuda", delta=0.02,
+                                         use_neigh_delta=False, dithering_sampling=True,
+                                         delta_eps=0.0005, seed=None):
+    """Drop-in for experiment_scripts/utils.py:92-169, built by one kernel.
+
+    ``vertices`` [M, 6 or 7] (xyz, normal, [neighbourhood delta]).  With
+    ``seed=None`` the sample indices and uniforms are drawn from torch's
+    generators exactly as the reference draws them (``torch.randperm`` on
+    ``device``, ``torch.rand`` on the CPU), so the batch equals the
+    reference's for the same generator state.  With an integer ``seed`` they
+    come from the kernel's counter-based generator (no host work; indices
+    drawn with replacement).  Returns {"on_surf": [pts, normals, sdfs]}.
+    """
+    V = vertices.detach().to(device=device, dtype=torch.float32).contiguous()
+    if not V.is_cuda:
+        raise RuntimeError("mplicits_gb300 builds training batches on a CUDA device only")
+    M, C = V.shape
+    n = min(int(n_on_surf), M)
+    idx = u = None
+    if seed is None:
+        if int(n_on_surf) == M:
+            idx = torch.arange(M, device=V.device)
+        else:
+            idx = torch.randperm(M, device=V.device)[:n_on_surf]
+        u = torch.rand((n, 3)).to(V.device)
+        idx = idx.to(torch.int64).contiguous()
+    rows = 3 * n if dithering_sampling else 2 * n
+    pts = torch.empty(rows, 3, dtype=torch.float32, device=V.device)
+    nrm = torch.empty(rows, 3, dtype=torch.float32, device=V.device)
+    sdf = torch.empty(rows, dtype=torch.float32, device=V.device)
+    flags = (capi.MPL_BATCH_NEIGH_DELTA if use_neigh_delta else 0) | \
+        (capi.MPL_BATCH_DITHER if dithering_sampling else 0)
+    capi.check(capi.load().mpl_train_batch(
+        capi.ptr(V), M, C, capi.ptr(idx), capi.ptr(u), n, float(delta), float(delta_eps), flags,
+        0 if seed is None else int(seed) & ((1 << 64) - 1), capi.ptr(pts), capi.ptr(nrm),
+        capi.ptr(sdf), capi.stream_ptr()), "mpl_train_batch")
+    return {"on_surf": [pts, nrm, sdf]}
+
+
 class ResidualTrainer:
     """Adam training of one level against frozen coarser levels.
 

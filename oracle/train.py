@@ -9,7 +9,8 @@ is carried in forward mode (a value row and three tangent rows per point,
 i3d/model.py:107-129 differentiated by hand) and the weight gradients come
 from one reverse pass over that graph.  Pinned by tests/golden/loss_fine.npz
 (the reference's own loss values and ``p.grad`` after ``loss.backward()``) and
-by central finite differences of the loss.
+by central finite differences of the loss.  ``training_batch`` restates the
+batch construction and is pinned bit for bit by tests/golden/train_batch.npz.
 
 Adam follows torch.optim.Adam's single-tensor update (no weight decay).
 """
@@ -150,3 +151,32 @@ def adam_update(p, g, m, v, step, lr=1e-4, beta1=0.9, beta2=0.999, eps=1e-8):
     bc2 = 1 - beta2 ** step
     denom = np.sqrt(v) / np.sqrt(bc2) + eps
     return p - (lr / bc1) * m / denom, m, v
+
+
+def training_batch(vertices, idx, u, delta, use_neigh_delta=False, dithering=True,
+                   delta_eps=0.0005):
+    """create_training_data_on_neighborhood (experiment_scripts/utils.py:
+    92-169) in float32 with the reference's operation order, given the
+    sample indices ``idx`` (the randperm prefix, or all rows) and the
+    uniforms ``u`` [n, 3] it draws.  Returns (pts, normals, sdf)."""
+    f = np.float32
+    surf = np.asarray(vertices, f)[np.asarray(idx)]
+    n = surf.shape[0]
+    u = np.asarray(u, f)
+    if use_neigh_delta:
+        dn = surf[:, -1:]
+    else:
+        dn = np.full((n, 1), f(delta_eps), f)
+    xyz, nrm = surf[:, :3], surf[:, 3:6]
+    off = xyz + (dn * u[:, 2:3]) * nrm
+    pts = [xyz, off]
+    normals = [nrm, nrm]
+    sdf = [np.zeros(n, f), (dn[:, 0] * u[:, 2]).astype(f)]
+    if dithering:
+        pd = u * f(delta)
+        pd = pd + (xyz + f(0.5 * delta) * nrm)
+        pts.append(pd)
+        normals.append(nrm)
+        sdf.append(np.full(n, -1.0, f))
+    return (np.concatenate(pts).astype(f), np.concatenate(normals).astype(f),
+            np.concatenate(sdf).astype(f))

@@ -221,3 +221,66 @@ def test_trainer_steps_follow_oracle(lib):
             # gradient is near zero may take the other sign in float32
             off = np.abs(got[2 * j + t] - params[j][t]) > 0.02 * moved
             assert off.mean() <= 0.01, (j, t, off.mean())
+
+
+def test_batch_kernel_matches_reference_bit_exact(lib):
+    """mpl_train_batch given the reference's own draws reproduces
+    create_training_data_on_neighborhood's batch bit for bit."""
+    from mplicits_gb300 import capi
+    d = golden("train_batch.npz")
+    V = torch.from_numpy(d["vertices"]).cuda()
+    for c in range(4):
+        idx = torch.from_numpy(d[f"c{c}.idx"]).cuda()
+        u = torch.from_numpy(d[f"c{c}.u"]).cuda()
+        n = idx.shape[0]
+        dither = bool(d[f"c{c}.dither"])
+        rows = 3 * n if dither else 2 * n
+        pts = torch.empty(rows, 3, device="cuda")
+        nrm = torch.empty(rows, 3, device="cuda")
+        sdf = torch.empty(rows, device="cuda")
+        flags = (capi.MPL_BATCH_NEIGH_DELTA if bool(d[f"c{c}.neigh"]) else 0) | \
+            (capi.MPL_BATCH_DITHER if dither else 0)
+        capi.check(lib.mpl_train_batch(capi.ptr(V), V.shape[0], V.shape[1], capi.ptr(idx),
+                                       capi.ptr(u), n, float(d[f"c{c}.delta"]), 0.0005, flags, 0,
+                                       capi.ptr(pts), capi.ptr(nrm), capi.ptr(sdf),
+                                       capi.stream_ptr()), "mpl_train_batch")
+        assert np.array_equal(pts.cpu().numpy(), d[f"c{c}.pts"]), c
+        assert np.array_equal(nrm.cpu().numpy(), d[f"c{c}.normals"]), c
+        assert np.array_equal(sdf.cpu().numpy(), d[f"c{c}.sdf"]), c
+    assert capi.device_status() == capi.MPL_OK
+
+
+def test_batch_drop_in_uses_torch_draws(lib):
+    from mplicits_gb300.train import create_training_data_on_neighborhood
+    d = golden("train_batch.npz")
+    V = torch.from_numpy(d["vertices"]).cuda()
+    torch.manual_seed(77)
+    out = create_training_data_on_neighborhood(V, 50, device="cuda", delta=0.01,
+                                               use_neigh_delta=True)
+    torch.manual_seed(77)
+    idx = torch.randperm(V.shape[0], device="cuda")[:50].cpu().numpy()
+    u = torch.rand((50, 3)).numpy()
+    ref = ot.training_batch(d["vertices"], idx, u, 0.01, True, True)
+    for got, want in zip(out["on_surf"], ref):
+        assert np.array_equal(got.cpu().numpy(), want)
+
+
+def test_batch_device_generator(lib):
+    from mplicits_gb300.train import create_training_data_on_neighborhood
+    d = golden("train_batch.npz")
+    V = torch.from_numpy(d["vertices"]).cuda()
+    a = create_training_data_on_neighborhood(V, 200, delta=0.01, seed=5)["on_surf"]
+    b = create_training_data_on_neighborhood(V, 200, delta=0.01, seed=5)["on_surf"]
+    c = create_training_data_on_neighborhood(V, 200, delta=0.01, seed=6)["on_surf"]
+    assert all(torch.equal(x, y) for x, y in zip(a, b))
+    assert not torch.equal(a[0], c[0])
+    pts, nrm, sdf = [t.cpu().numpy() for t in a]
+    vset = {tuple(r) for r in d["vertices"][:, :3].tolist()}
+    assert all(tuple(r) in vset for r in pts[:200].tolist())
+    assert np.all(sdf[:200] == 0) and np.all(sdf[400:] == -1)
+    assert np.all((sdf[200:400] >= 0) & (sdf[200:400] < 0.0005))
+    # offset rows lie on the normal line at the recorded distance
+    off = pts[200:400] - pts[:200]
+    assert np.allclose(off, sdf[200:400, None] * nrm[:200], atol=1e-7)
+    dith = pts[400:] - pts[:200] - 0.005 * nrm[:200]
+    assert np.all((dith >= -1e-6) & (dith < 0.01 + 1e-6))

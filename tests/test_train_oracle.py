@@ -72,3 +72,14 @@ def test_oracle_adam_matches_torch():
         opt.step()
         po, m, v = ot.adam_update(po, g, m, v, step, lr=1e-3)
         assert np.allclose(p.detach().numpy(), po, rtol=0, atol=1e-12)
+
+
+def test_oracle_training_batch_matches_reference():
+    d = golden("train_batch.npz")
+    for c in range(4):
+        p, nr, s = ot.training_batch(d["vertices"], d[f"c{c}.idx"], d[f"c{c}.u"],
+                                     float(d[f"c{c}.delta"]), bool(d[f"c{c}.neigh"]),
+                                     bool(d[f"c{c}.dither"]))
+        assert np.array_equal(p, d[f"c{c}.pts"]), c
+        assert np.array_equal(nr, d[f"c{c}.normals"]), c
+        assert np.array_equal(s, d[f"c{c}.sdf"]), c
