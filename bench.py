@@ -63,6 +63,7 @@ def parse():
                     help="epilogue unit width of the BF16 kernel (default: the library's)")
     ap.add_argument("--skip-train", action="store_true")
     ap.add_argument("--skip-trace", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="time only the BF16 steps (for profiler runs) and print a short line")
     return ap.parse_args()
@@ -485,6 +486,102 @@ def trace_cpu_baseline(levels_np, W=192, H=108):
             "sample": f"one {W}x{H} frame of the first orbit camera, float64 numpy oracle"}
 
 
+def level_flop(width, hidden=3):
+    return 2 * (3 * width + (hidden - 1) * width * width + width)
+
+
+def batch_workload(device, n_models=64, lo=1e4, hi=2e6, seed=11):
+    """64 independent three-level models, widths 128 or 256 drawn uniformly,
+    3 hidden layers, each level from its own seed (the reference's init);
+    per model three nested point lists with sizes log-uniform in [lo, hi]
+    (sorted: level 0 on the largest, levels 1 and 2 on index sublists)."""
+    import torch
+    from mplicits_gb300.batch import BatchEntry
+    from mplicits_gb300.model import SIREN
+    rng = np.random.default_rng(seed)
+    entries = []
+    for mi in range(n_models):
+        width = int(rng.choice([128, 256]))
+        sizes = sorted(np.exp(rng.uniform(np.log(lo), np.log(hi), 3)).astype(np.int64),
+                       reverse=True)
+        n0 = int(sizes[0])
+        g = torch.Generator(device).manual_seed(seed * 1000 + mi)
+        x = torch.rand(n0, 3, device=device, generator=g) * 2 - 1
+        perm = torch.randperm(n0, device=device, generator=g).to(torch.int32)
+        for lv in range(3):
+            torch.manual_seed(seed * 100000 + mi * 3 + lv)
+            m = SIREN(3, 1, [width] * 3, w0=30, precision="bf16").to(device).eval()
+            n = int(sizes[lv])
+            S = torch.empty(n0, device=device)
+            idx = None if lv == 0 else perm[:n].contiguous()
+            entries.append(BatchEntry(m, S, x=x, index=idx, n=n))
+    return entries
+
+
+def batch_bench(device, K, W):
+    """One persistent graph-captured launch over all 192 levels against
+    per-level launches of the single-level kernels (BF16, and plain FP32)."""
+    import ctypes
+    import torch
+    from mplicits_gb300 import capi
+    from mplicits_gb300.batch import BatchedLevels
+    entries = batch_workload(device)
+    pts = sum(e.n for e in entries)
+    flop = sum(e.n * level_flop(e.model.linears()[0].out_features) for e in entries)
+    bl = BatchedLevels(entries, "bf16")
+    t0 = time.perf_counter()
+    cfg, tuned_ms = bl.autotune(repeats=3, cache=False)
+    tune_s = time.perf_counter() - t0
+    bl.capture()
+    lib = capi.load()
+
+    def per_level(precision):
+        st = capi.stream_ptr()
+        for e in entries:
+            net, packed = e.model.packed()
+            p = capi.MplPoints(kind=capi.MPL_POINTS_XYZ, xyz=e.x.data_ptr())
+            capi.check(lib.mpl_level_forward(
+                ctypes.byref(net), capi.ptr(packed), ctypes.byref(p), capi.ptr(e.index), None,
+                e.n, capi.ptr(e.S), capi.MPL_STORE, None, capi.PRECISIONS[precision], st),
+                "mpl_level_forward")
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(k):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k
+
+    ms_batch = timed(bl.replay, K, W)
+    capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, cfg.epilogue_unit)
+    try:
+        ms_bf16 = timed(lambda: per_level("bf16"), K, W)
+    finally:
+        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 16)
+    ms_fp32 = timed(lambda: per_level("fp32"), 1, 1)
+    peak_tf, _, src = peaks()
+    widths = [e.model.linears()[0].out_features for e in entries[::3]]
+    return {"workload": "64 three-level models (192 levels), widths 128/256 uniform, 3 hidden "
+                        "layers, distinct seeds, nested point lists log-uniform in [1e4, 2e6]",
+            "points_per_step": pts, "flop_per_step": flop,
+            "models_width_256": int(sum(w == 256 for w in widths)),
+            "value": pts / (ms_batch * 1e-3), "unit": "pts/s", "ms_per_step": ms_batch,
+            "achieved_tflops": flop / (ms_batch * 1e-3) / 1e12,
+            "frac_of_peak": flop / (ms_batch * 1e-3) / 1e12 / peak_tf,
+            "peak_source": f"{src} bf16 sustained",
+            "autotuned": {"epilogue_unit": cfg.epilogue_unit, "stages": cfg.stages,
+                          "ctas": cfg.ctas, "best_ms": tuned_ms, "tuning_s": round(tune_s, 3)},
+            "per_level_bf16_ms": ms_bf16, "per_level_fp32_ms": ms_fp32,
+            "speedup_vs_fp32_per_model": ms_fp32 / ms_batch,
+            "speedup_vs_bf16_per_level": ms_bf16 / ms_batch,
+            "gpu_launches_per_step": 1}
+
+
 def run_reference(args):
     rank, world, _ = rank_info()
     if rank != 0:
@@ -600,6 +697,10 @@ def main():
         if rank == 0 and not args.skip_cpu:
             tracing["cpu_baseline"] = trace_cpu_baseline(levels_np)
 
+    batched = None
+    if not args.skip_batch:
+        batched = batch_bench(device, K, W)
+
     # ---- roofline of the dominant kernel (level 0 over the full grid)
     peak_tf, hbm, src = peaks()
     achieved_tf = FLOP_PER_POINT * N ** 3 / (l0_ms * 1e-3) / 1e12
@@ -648,6 +749,7 @@ def main():
             "cpu_baseline": cpu,
             "training": training,
             "sphere_tracing": tracing,
+            "batched_models": batched,
             "gpu_launches": K * KERNEL_LAUNCHES_PER_STEP,
             "clocks": clk.summary(),
         }

@@ -291,6 +291,63 @@ int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* g
                   float* const* exp_avg_dev, float* const* exp_avg_sq_dev, const int64_t* numel,
                   float lr, float beta1, float beta2, float eps, int64_t step, void* stream);
 
+/* ---- batched evaluation of many levels of many models ------------------- */
+/* No single reference entry point: this replaces the reference's one launch
+ * chain per model and per level (renderer/cuda/gemms.cu:5-192 NeuralImplicit,
+ * and the per-level loop of i3d/meshing.py:212-236) by one persistent launch
+ * over all entries.  Entries are levels with 1 or 2 hidden GEMMs of width
+ * <= 256 (padded widths 64/128/256 may mix); each runs on its own point list
+ * (points + optional index list, count optionally on the device) and stores
+ * or accumulates into its own S.  Tensor-core operands only (MPL_BF16 or
+ * MPL_F16); results equal mpl_level_forward of the same entry bit for bit
+ * under the same epilogue unit width. */
+#define MPL_BATCH_MAX_ENTRIES 1024
+
+typedef struct {
+  MplNet net;
+  const void* packed_dev; /* mpl_net_pack image, 256-byte aligned */
+  MplPoints points;
+  const int32_t* index_dev; /* nullable: point q is points[index[q]]  */
+  const int32_t* n_dev;     /* nullable: device count, min(n, *n_dev)  */
+  int64_t n;
+  float* S_dev;
+  int32_t store_mode;
+  int32_t reserved;
+} MplBatchEntry;
+
+typedef struct {
+  void* workspace_dev; /* the device entry table */
+  int32_t count;
+  int32_t precision;
+} MplBatchPlan;
+
+typedef struct {
+  int32_t epilogue_unit; /* 16 or 32 features per epilogue warp (0: 16)   */
+  int32_t stages;        /* weight-ring depth, 2 or 3 (0: 3)               */
+  int32_t ctas;          /* persistent CTAs (0: one per SM)                */
+  int32_t reserved;
+} MplBatchConfig;
+
+/* Bytes of the device workspace that holds a plan of `count` entries. */
+int mpl_batch_workspace_bytes(int32_t count, int64_t* bytes);
+/* Validates the entries and writes the device entry table into `workspace`
+ * (256-byte aligned).  Synchronises `stream` (the host table is released on
+ * return); call it outside stream capture.  Device pointers in the entries
+ * must stay valid while the plan is used. */
+int mpl_batch_prepare(const MplBatchEntry* entries, int32_t count, int32_t precision,
+                      void* workspace_dev, int64_t workspace_bytes, MplBatchPlan* plan,
+                      void* stream);
+/* One persistent launch over every tile of every entry; no host sync, so it
+ * can be captured in a CUDA graph.  config nullable (defaults). */
+int mpl_batch_run(const MplBatchPlan* plan, const MplBatchConfig* config, void* stream);
+/* Times every configuration (epilogue unit x weight-ring depth) on the plan
+ * itself, `repeats` runs each after a warm-up run, and returns the fastest
+ * (minimum time) in *best and *best_ms.  Synchronises; the entries' outputs
+ * afterwards hold the result of repeated runs (re-initialise S of
+ * MPL_ACCUMULATE entries before the real run). */
+int mpl_batch_autotune(const MplBatchPlan* plan, int32_t repeats, MplBatchConfig* best,
+                       float* best_ms, void* stream);
+
 /* ---- tuning ------------------------------------------------------------- */
 
 /* Process-wide kernel options (read at each launch). */

@@ -68,6 +68,34 @@ class MplCamera(ctypes.Structure):
                 ("height", ctypes.c_int32)]
 
 
+class MplBatchEntry(ctypes.Structure):
+    _fields_ = [("net", MplNet),
+                ("packed_dev", ctypes.c_void_p),
+                ("points", MplPoints),
+                ("index_dev", ctypes.c_void_p),
+                ("n_dev", ctypes.c_void_p),
+                ("n", ctypes.c_int64),
+                ("S_dev", ctypes.c_void_p),
+                ("store_mode", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class MplBatchPlan(ctypes.Structure):
+    _fields_ = [("workspace_dev", ctypes.c_void_p),
+                ("count", ctypes.c_int32),
+                ("precision", ctypes.c_int32)]
+
+
+class MplBatchConfig(ctypes.Structure):
+    _fields_ = [("epilogue_unit", ctypes.c_int32),
+                ("stages", ctypes.c_int32),
+                ("ctas", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+MPL_BATCH_MAX_ENTRIES = 1024
+
+
 # (name, restype, argtypes) of every exported symbol; tests check that the
 # library exports exactly what include/mplicits.h declares.
 _P = ctypes.c_void_p
@@ -102,6 +130,14 @@ SIGNATURES = {
     "mpl_train_batch": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _F, _F, _I32,
                                        ctypes.c_uint64, _P, _P, _P, _P]),
     "mpl_adam_step": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _F, _F, _F, _F, _I64, _P]),
+    "mpl_batch_workspace_bytes": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
+    "mpl_batch_prepare": (ctypes.c_int, [ctypes.POINTER(MplBatchEntry), _I32, _I32, _P, _I64,
+                                         ctypes.POINTER(MplBatchPlan), _P]),
+    "mpl_batch_run": (ctypes.c_int, [ctypes.POINTER(MplBatchPlan),
+                                     ctypes.POINTER(MplBatchConfig), _P]),
+    "mpl_batch_autotune": (ctypes.c_int, [ctypes.POINTER(MplBatchPlan), _I32,
+                                          ctypes.POINTER(MplBatchConfig),
+                                          ctypes.POINTER(ctypes.c_float), _P]),
     "mpl_set_option": (ctypes.c_int, [_I32, _I64]),
     "mpl_get_option": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
     "mpl_status_string": (ctypes.c_char_p, [ctypes.c_int]),
