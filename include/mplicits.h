@@ -265,6 +265,29 @@ int mpl_train_backward(const MplNet* net, const void* packed_dev, const float* x
                        const float* pre_dev, const float* seeds_dev, float* da_dev,
                        float* const* dW_dev, float* const* db_dev, void* stream);
 
+/* Bytes of the device scratch of mpl_train_tc_step for n points: the BF16
+ * activation and adjoint tiles of every layer, 2 * (hidden GEMMs + 1) *
+ * rows * padded width * 2 with rows = 4 * n rounded up to 128. */
+int mpl_train_tc_scratch_bytes(const MplNet* net, int64_t n, int64_t* bytes);
+
+/* The training step of one level on the tensor cores (BF16 operands, FP32
+ * accumulation, FP32 master weights outside): forward in forward mode, the
+ * residual loss of the fine trainer with S = f + f_frozen and
+ * G = df/dx + g_frozen (as mpl_train_loss, sums into loss_sums[3], seeds
+ * [n, 4] written, 16-byte aligned), the backward through the forward-mode
+ * graph (double backward included) and every weight gradient, ADDED into
+ * the padded buffers dW[l] / db[l] of mpl_train_backward.  Replaces the
+ * reference trainer's forward, loss_add_detail_fine and loss.backward()
+ * (experiment_scripts/train_sdf_on_neighborhood_fine.py:247-250,
+ * i3d/loss_functions.py:347-394).  Levels with 1 or 2 hidden GEMMs of padded
+ * width 128 or 256. */
+int mpl_train_tc_step(const MplNet* net, const void* packed_dev, const float* xyz_dev, int64_t n,
+                      const float* f_frozen_dev, const float* g_frozen_dev,
+                      const float* gt_sdf_dev, const float* gt_normals_dev, float w_sdf,
+                      float w_normal, float w_eikonal, void* scratch_dev, int64_t scratch_bytes,
+                      float* seeds_dev, float* loss_sums_dev, float* const* dW_dev,
+                      float* const* db_dev, void* stream);
+
 /* Flags of mpl_train_batch. */
 #define MPL_BATCH_NEIGH_DELTA 1 /* offset scale from the last column (use_neigh_delta) */
 #define MPL_BATCH_DITHER 2      /* append the dithered rows (dithering_sampling)      */

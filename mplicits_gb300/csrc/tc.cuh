@@ -34,6 +34,15 @@ __host__ __device__ constexpr uint32_t idesc_f16kind_f32(int M, int N, uint32_t 
          ((uint32_t)(M >> 4) << 24);
 }
 
+// The same with either operand MN-major (bit 15: A, bit 16: B).  An
+// MN-major operand without swizzle is tiled in core matrices of 8 K-rows x
+// 16 bytes (8 consecutive M/N elements per row); in its descriptor the
+// leading-dimension offset steps along K and the stride offset along M/N.
+__host__ __device__ constexpr uint32_t idesc_f16kind_f32_major(int M, int N, uint32_t fmt,
+                                                               bool a_mn, bool b_mn) {
+  return idesc_f16kind_f32(M, N, fmt) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16);
+}
+
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
   return idesc_f16kind_f32(M, N, 1u);
 }

@@ -263,33 +263,42 @@ __global__ void __launch_bounds__(256) train_wgrad_hidden_kernel(const TrainArgs
 
 // Layer 0 (3 inputs): dW0[j][c] += sum_q da_v[j] x_qc + da_tc[j]; db0[j] += da_v[j].
 // Output layer: dWL[j] += sum_rows seed_row out_(L-1)[row][j]; dbL += seed_v.
-__global__ void train_wgrad_ends_kernel(const TrainArgs a, int WP, float* dW0, float* db0,
-                                        float* dWL, float* dbL) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+// Thread j of a block, 8 points per step; each block covers a contiguous
+// point range and adds its partial sums atomically.
+__global__ void __launch_bounds__(256) train_wgrad_ends_kernel(const TrainArgs a, int WP,
+                                                               float* dW0, float* db0, float* dWL,
+                                                               float* dbL) {
   const int nh = a.lay.nh;
-  const int64_t per = (a.n + gridDim.y - 1) / gridDim.y;
-  const int64_t q_begin = blockIdx.y * per;
+  const int64_t per = (a.n + gridDim.x - 1) / gridDim.x;
+  const int64_t q_begin = blockIdx.x * per;
   const int64_t q_end = q_begin + per < a.n ? q_begin + per : a.n;
-  if (j < WP) {
-    float w0[3] = {0.f, 0.f, 0.f}, b0 = 0.f, wl = 0.f;
-    const float om = a.omega[nh];
+  const float om = a.omega[nh];
+  for (int j = threadIdx.x; j < WP; j += blockDim.x) {
+    float w0x = 0.f, w0y = 0.f, w0z = 0.f, b0 = 0.f, wl = 0.f;
     for (int64_t q = q_begin; q < q_end; ++q) {
       const float* d = a.da + (q * 4) * WP;  // layer 0
       const float dv = d[j];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) w0[c] = __fadd_rn(w0[c], __fmaf_rn(dv, a.xyz[3 * q + c], d[(1 + c) * WP + j]));
+      w0x = __fadd_rn(w0x, __fmaf_rn(dv, a.xyz[3 * q + 0], d[1 * WP + j]));
+      w0y = __fadd_rn(w0y, __fmaf_rn(dv, a.xyz[3 * q + 1], d[2 * WP + j]));
+      w0z = __fadd_rn(w0z, __fmaf_rn(dv, a.xyz[3 * q + 2], d[3 * WP + j]));
       b0 = __fadd_rn(b0, dv);
       const float* pr = a.pre + (((int64_t)nh * a.n + q) * 4) * WP;
-      const float* sd = a.seed + q * 4;
-#pragma unroll
-      for (int ch = 0; ch < 4; ++ch) wl = __fmaf_rn(sd[ch], layer_input(pr, WP, ch, j, om), wl);
+      const float4 sd = *reinterpret_cast<const float4*>(a.seed + q * 4);
+      float s, c;
+      sincosf(__fmul_rn(om, pr[j]), &s, &c);
+      const float oc = __fmul_rn(om, c);
+      float t = __fmul_rn(sd.y, pr[1 * WP + j]);
+      t = __fmaf_rn(sd.z, pr[2 * WP + j], t);
+      t = __fmaf_rn(sd.w, pr[3 * WP + j], t);
+      wl = __fmaf_rn(sd.x, s, __fmaf_rn(oc, t, wl));
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) atomicAdd(&dW0[j * 3 + c], w0[c]);
+    atomicAdd(&dW0[j * 3 + 0], w0x);
+    atomicAdd(&dW0[j * 3 + 1], w0y);
+    atomicAdd(&dW0[j * 3 + 2], w0z);
     atomicAdd(&db0[j], b0);
     atomicAdd(&dWL[j], wl);
   }
-  if (j == 0) {
+  if (threadIdx.x == 0) {
     float b = 0.f;
     for (int64_t q = q_begin; q < q_end; ++q) b = __fadd_rn(b, a.seed[q * 4]);
     atomicAdd(dbL, b);
@@ -551,8 +560,10 @@ extern "C" int mpl_train_backward(const MplNet* net, const void* packed, const f
     train_wgrad_hidden_kernel<<<grid, 256, 0, s>>>(t, l, WP, dW[l], db[l]);
     MPL_LAUNCH_CHECK();
   }
-  dim3 g2((WP + 127) / 128, splits < 1 ? 1 : splits);
-  train_wgrad_ends_kernel<<<g2, 128, 0, s>>>(t, WP, dW[0], db[0], dW[L - 1], db[L - 1]);
+  // about 64 points per block
+  const int64_t eb = (n + 63) / 64 < 4096 ? (n + 63) / 64 : 4096;
+  train_wgrad_ends_kernel<<<(unsigned)eb, WP < 256 ? WP : 256, 0, s>>>(t, WP, dW[0], db[0],
+                                                                       dW[L - 1], db[L - 1]);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }

@@ -209,7 +209,10 @@ class ResidualTrainer:
     """
 
     def __init__(self, model, frozen=(), lr=1e-4, betas=(0.9, 0.999), eps=1e-8,
-                 constraint_weights=None):
+                 constraint_weights=None, precision="fp32"):
+        if precision not in ("fp32", "bf16"):
+            raise ValueError("precision is 'fp32' (plain kernels) or 'bf16' (tensor cores)")
+        self.precision = precision
         self.model = model
         self.frozen = list(frozen)
         self.lr, self.betas, self.eps = lr, betas, eps
@@ -236,7 +239,9 @@ class ResidualTrainer:
             Ff = torch.empty(n, dtype=torch.float32, device=x.device)
             Gf = torch.empty(n, 3, dtype=torch.float32, device=x.device)
             for i, m in enumerate(self.frozen):
-                level_gradient(m, x, S=Ff, G=Gf, accumulate=i > 0, precision="fp32")
+                level_gradient(m, x, S=Ff, G=Gf, accumulate=i > 0, precision=self.precision)
+        if self.precision == "bf16":
+            return self._tc_loss_and_grads(x, normals, sdf, Ff, Gf)
         sc = _scratch(self.model, n, x.device)
         _forward_with_scratch(self.model, x, sc)
         w = self.weights
@@ -245,6 +250,42 @@ class ResidualTrainer:
             capi.ptr(normals), w["sdf_constraint"], w["normal_constraint"], w["grad_constraint"],
             capi.ptr(sc.seeds[:n]), capi.ptr(self.loss_sums), capi.stream_ptr()), "mpl_train_loss")
         _backward(self.model, x, sc)
+        grads = _unpad(self.model, sc)
+        scale = torch.tensor([w["sdf_constraint"], w["normal_constraint"], w["grad_constraint"]],
+                             dtype=torch.float32, device=x.device) / n
+        return self.loss_sums * scale, grads
+
+    def _tc_loss_and_grads(self, x, normals, sdf, Ff, Gf):
+        """One mpl_train_tc_step: forward, loss, backward and weight gradients
+        on the tensor cores."""
+        n = x.shape[0]
+        lib = capi.load()
+        net, packed = self.model.packed()
+        nb = ctypes.c_int64(0)
+        capi.check(lib.mpl_train_tc_scratch_bytes(ctypes.byref(net), n, ctypes.byref(nb)),
+                   "mpl_train_tc_scratch_bytes")
+        buf = getattr(self, "_tc_buf", None)
+        if buf is None or buf.numel() < nb.value + 256:
+            buf = torch.empty(nb.value + 256, dtype=torch.uint8, device=x.device)
+            self._tc_buf = buf
+        off = (-buf.data_ptr()) % 256
+        sc = _scratch(self.model, 1, x.device)  # the padded gradient buffers
+        seeds = getattr(self, "_tc_seeds", None)
+        if seeds is None or seeds.shape[0] < n:
+            seeds = torch.empty(n, 4, dtype=torch.float32, device=x.device)
+            self._tc_seeds = seeds
+        for t in sc.dW + sc.db:
+            t.zero_()
+        P = ctypes.c_void_p
+        dW = (P * len(sc.dW))(*[t.data_ptr() for t in sc.dW])
+        db = (P * len(sc.db))(*[t.data_ptr() for t in sc.db])
+        w = self.weights
+        capi.check(lib.mpl_train_tc_step(
+            ctypes.byref(net), capi.ptr(packed), capi.ptr(x), n, capi.ptr(Ff), capi.ptr(Gf),
+            capi.ptr(sdf), capi.ptr(normals), w["sdf_constraint"], w["normal_constraint"],
+            w["grad_constraint"], ctypes.c_void_p(buf.data_ptr() + off), nb.value,
+            capi.ptr(seeds), capi.ptr(self.loss_sums), dW, db, capi.stream_ptr()),
+            "mpl_train_tc_step")
         grads = _unpad(self.model, sc)
         scale = torch.tensor([w["sdf_constraint"], w["normal_constraint"], w["grad_constraint"]],
                              dtype=torch.float32, device=x.device) / n
