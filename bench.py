@@ -371,7 +371,7 @@ TRAIN_SURFACE = 1 << 16  # surface samples per batch; rows = 3x (surface, offset
 # layers over the four rows
 _FWD_TANGENT = 2 * (3 * 256 + 2 * 256 * 256 + 256) + 3 * 2 * (2 * 256 * 256 + 256)
 TRAIN_FLOP_PER_ROW = 3 * _FWD_TANGENT + 2 * (2 * 4 * 2 * 256 * 256)
-TRAIN_LAUNCHES_PER_STEP = 10  # batch, 2 frozen gradients, forward, loss, backward (4), Adam
+TRAIN_LAUNCHES_PER_STEP = 7  # batch, 2 frozen gradients, fused step, weight GEMM, ends, Adam
 
 
 def train_surface(n=1 << 18, seed=1):
@@ -380,15 +380,15 @@ def train_surface(n=1 << 18, seed=1):
     return np.concatenate([pts, nrm], 1).astype(np.float32)
 
 
-def train_bench(levels_np, device, K, W):
+def train_bench(levels_np, device, K, W, precision="bf16"):
     """The fine-level training step: batch construction on the device, the
     frozen coarse and medium levels' f and df/dx, the trainable level's
-    forward, loss, hand-written backward and Adam."""
+    forward, loss, hand-written backward and Adam (FP32 master weights)."""
     import torch
     from mplicits_gb300.train import ResidualTrainer, create_training_data_on_neighborhood
     V = torch.from_numpy(train_surface()).to(device)
-    models = make_models(levels_np, "fp32", device)
-    tr = ResidualTrainer(models[2], models[:2], lr=1e-4)
+    models = make_models(levels_np, precision, device)
+    tr = ResidualTrainer(models[2], models[:2], lr=1e-4, precision=precision)
     it = [0]
 
     def step():
@@ -411,12 +411,13 @@ def train_bench(levels_np, device, K, W):
     return {"workload": f"fine-level residual training step: {TRAIN_SURFACE} surface samples "
                         f"-> {rows} rows (surface, normal offset, delta1-dithered), level "
                         "3->256x3->1 trainable, coarse and medium frozen, losses of "
-                        "loss_add_detail_fine, Adam lr 1e-4, FP32",
+                        "loss_add_detail_fine, Adam lr 1e-4, FP32 master weights",
             "value": rows / (ms * 1e-3), "unit": "rows/s", "ms_per_step": ms, "steps": K,
-            "warmup": W, "dtype": "f32", "flop_per_row": TRAIN_FLOP_PER_ROW,
+            "warmup": W, "dtype": "bf16" if precision == "bf16" else "f32",
+            "flop_per_row": TRAIN_FLOP_PER_ROW,
             "achieved_tflops": TRAIN_FLOP_PER_ROW * rows / (ms * 1e-3) / 1e12,
             "last_losses": [float(x) for x in losses.cpu()],
-            "gpu_launches": K * TRAIN_LAUNCHES_PER_STEP}
+            "gpu_launches": K * (TRAIN_LAUNCHES_PER_STEP if precision == "bf16" else 10)}
 
 
 def train_cpu_baseline(levels_np, rows=3072, steps=3):
@@ -682,7 +683,9 @@ def main():
     # ---- the training step and the sphere tracer
     training = tracing = None
     if not args.skip_train:
-        training = train_bench(levels_np, device, K, W)
+        training = train_bench(levels_np, device, K, W, "bf16")
+        training["fp32"] = train_bench(levels_np, device, K, W, "fp32")
+        training["speedup_bf16_vs_fp32"] = training["fp32"]["ms_per_step"] / training["ms_per_step"]
         if rank == 0 and not args.skip_cpu:
             training["cpu_baseline"] = train_cpu_baseline(levels_np)
     if not args.skip_trace:

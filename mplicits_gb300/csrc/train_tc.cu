@@ -683,8 +683,11 @@ __global__ void __launch_bounds__(192, 1) train_tc_wgrad_kernel(const WgArgs w) 
 //   db_l[j]  += omega_l * sum_points dz_l[value row][j]        (l = 0..nh)
 //   dW0[j][c] += omega_0 * sum_points (dz_0[v][j] x_c + dz_0[t_c][j])
 //   dWL[j]   += sum_rows seed_row * s_nh[row][j],  dbL += sum_points seed_v.
-// Thread (f8, slot): features 8 f8 .. 8 f8 + 7 of 8 rows of each 64-row
-// block; block-level sums in shared memory, then one atomic per value.
+// Block (f8, split): features 8 f8 .. 8 f8 + 7.  Each warp walks 64-row
+// blocks, lane l taking rows l and l + 32, so a warp reads 512 contiguous
+// bytes per operand (one 8-feature column of a block is 1 KiB contiguous).
+// Lanes keep their partial sums across blocks; one warp reduction and one
+// atomic per value at the end.
 // ---------------------------------------------------------------------------
 struct EndsArgs {
   const __nv_bfloat16* dz;  // layer 0 of the dz tiles; layer l at + l * lstride
@@ -700,109 +703,97 @@ struct EndsArgs {
   float* dbL;
 };
 
-__global__ void __launch_bounds__(256) train_tc_ends_kernel(const EndsArgs e) {
-  extern __shared__ float acc_s[];  // [(nh + 1) + 3 + 1][WP] + 1
+__device__ __forceinline__ void add8(float (&acc)[8], const uint4& v) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(h[i]);
+    acc[2 * i] += f.x;
+    acc[2 * i + 1] += f.y;
+  }
+}
+
+__device__ __forceinline__ void fma8(float (&acc)[8], const uint4& v, float s) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(h[i]);
+    acc[2 * i] = __fmaf_rn(s, f.x, acc[2 * i]);
+    acc[2 * i + 1] = __fmaf_rn(s, f.y, acc[2 * i + 1]);
+  }
+}
+
+constexpr int kEndsWarps = 8;
+constexpr int kEndsQ = 3 + 3 + 1;  // db_0..db_2, dW0 x/y/z, dWL
+
+__global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const EndsArgs e) {
+  __shared__ float part[kEndsWarps][kEndsQ * 8 + 1];
   const int WP = e.WP, nh = e.nh;
-  const int nf8 = WP / 8;
-  const int nq = (nh + 1) + 3 + 1;  // db_0..db_nh, dW0 x/y/z, dWL
-  for (int i = threadIdx.x; i < nq * WP + 1; i += blockDim.x) acc_s[i] = 0.f;
-  __syncthreads();
-  const int f8 = threadIdx.x % nf8;
-  const int slot = threadIdx.x / nf8;
-  const int nslots = blockDim.x / nf8;
-  constexpr int kL = 3;  // db_0 .. db_nh, nh <= 2
-  float db[kL][8];
-  float w0[3][8], wl[8];
+  const int f8 = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float acc[kEndsQ][8];
   float dbl = 0.f;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
+  for (int qq = 0; qq < kEndsQ; ++qq)
 #pragma unroll
-    for (int l = 0; l < kL; ++l) db[l][i] = 0.f;
-    w0[0][i] = w0[1][i] = w0[2][i] = 0.f;
-    wl[i] = 0.f;
-  }
-  if (slot < nslots) {
-    for (int64_t b = blockIdx.x; b < e.nblocks; b += gridDim.x) {
-      for (int r = slot; r < 64; r += nslots) {
-        const int64_t row = b * 64 + r;
-        const int64_t p = row >> 2;
-        if (p >= e.n) break;
-        const int ch = (int)(row & 3);
-        const int64_t off = wg_offset(row, f8 * 8, WP);
-        const float sd = e.seeds[4 * p + ch];
-        {
-          const uint4 sv = *reinterpret_cast<const uint4*>(e.s_last + off);
-          const __nv_bfloat162* s2 = reinterpret_cast<const __nv_bfloat162*>(&sv);
+    for (int i = 0; i < 8; ++i) acc[qq][i] = 0.f;
+  for (int64_t b = (int64_t)blockIdx.y * kEndsWarps + warp; b < e.nblocks;
+       b += (int64_t)gridDim.y * kEndsWarps) {
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const float2 f = __bfloat1622float2(s2[i]);
-            wl[2 * i] = __fmaf_rn(sd, f.x, wl[2 * i]);
-            wl[2 * i + 1] = __fmaf_rn(sd, f.y, wl[2 * i + 1]);
-          }
-        }
-        const uint4 dv = *reinterpret_cast<const uint4*>(e.dz + off);
-        const __nv_bfloat162* d2 = reinterpret_cast<const __nv_bfloat162*>(&dv);
-        if (ch == 0) {
-          const float px = e.xyz[3 * p], py = e.xyz[3 * p + 1], pz = e.xyz[3 * p + 2];
-          if (f8 == 0) dbl += sd;
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const float2 f = __bfloat1622float2(d2[i]);
-            db[0][2 * i] += f.x;
-            db[0][2 * i + 1] += f.y;
-            w0[0][2 * i] = __fmaf_rn(f.x, px, w0[0][2 * i]);
-            w0[0][2 * i + 1] = __fmaf_rn(f.y, px, w0[0][2 * i + 1]);
-            w0[1][2 * i] = __fmaf_rn(f.x, py, w0[1][2 * i]);
-            w0[1][2 * i + 1] = __fmaf_rn(f.y, py, w0[1][2 * i + 1]);
-            w0[2][2 * i] = __fmaf_rn(f.x, pz, w0[2][2 * i]);
-            w0[2][2 * i + 1] = __fmaf_rn(f.y, pz, w0[2][2 * i + 1]);
-          }
-#pragma unroll
-          for (int l = 1; l < kL; ++l) {
-            if (l > nh) break;
-            const uint4 lv = *reinterpret_cast<const uint4*>(e.dz + l * e.lstride + off);
-            const __nv_bfloat162* l2 = reinterpret_cast<const __nv_bfloat162*>(&lv);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              const float2 f = __bfloat1622float2(l2[i]);
-              db[l][2 * i] += f.x;
-              db[l][2 * i + 1] += f.y;
-            }
-          }
-        } else {
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const float2 f = __bfloat1622float2(d2[i]);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              if (c == ch - 1) {
-                w0[c][2 * i] += f.x;
-                w0[c][2 * i + 1] += f.y;
-              }
-            }
-          }
-        }
+    for (int half = 0; half < 2; ++half) {
+      const int64_t row = b * 64 + lane + 32 * half;
+      const int64_t p = row >> 2;
+      if (p >= e.n) continue;
+      const int ch = (int)(row & 3);
+      const int64_t off = wg_offset(row, f8 * 8, WP);
+      const float sd = e.seeds[4 * p + ch];
+      fma8(acc[6], *reinterpret_cast<const uint4*>(e.s_last + off), sd);
+      const uint4 dv = *reinterpret_cast<const uint4*>(e.dz + off);
+      if (ch == 0) {
+        dbl += sd;
+        add8(acc[0], dv);
+        fma8(acc[3], dv, e.xyz[3 * p + 0]);
+        fma8(acc[4], dv, e.xyz[3 * p + 1]);
+        fma8(acc[5], dv, e.xyz[3 * p + 2]);
+        add8(acc[1], *reinterpret_cast<const uint4*>(e.dz + e.lstride + off));
+        if (nh > 1) add8(acc[2], *reinterpret_cast<const uint4*>(e.dz + 2 * e.lstride + off));
+      } else if (ch == 1) {
+        add8(acc[3], dv);
+      } else if (ch == 2) {
+        add8(acc[4], dv);
+      } else {
+        add8(acc[5], dv);
       }
     }
+  }
+#pragma unroll
+  for (int qq = 0; qq < kEndsQ; ++qq)
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const int j = f8 * 8 + i;
+      float v = acc[qq][i];
 #pragma unroll
-      for (int l = 0; l < kL; ++l)
-        if (l <= nh) atomicAdd(&acc_s[l * WP + j], db[l][i]);
-      for (int c = 0; c < 3; ++c) atomicAdd(&acc_s[(nh + 1 + c) * WP + j], w0[c][i]);
-      atomicAdd(&acc_s[(nh + 4) * WP + j], wl[i]);
+      for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) part[warp][qq * 8 + i] = v;
     }
-    if (f8 == 0) atomicAdd(&acc_s[nq * WP], dbl);
-  }
+  for (int o = 16; o >= 1; o >>= 1) dbl += __shfl_xor_sync(0xffffffffu, dbl, o);
+  if (lane == 0) part[warp][kEndsQ * 8] = dbl;
   __syncthreads();
-  for (int j = threadIdx.x; j < WP; j += blockDim.x) {
-    for (int l = 0; l <= nh; ++l) atomicAdd(&e.db[l][j], __fmul_rn(e.omega[l], acc_s[l * WP + j]));
-    for (int c = 0; c < 3; ++c)
-      atomicAdd(&e.dW0[j * 3 + c], __fmul_rn(e.omega[0], acc_s[(nh + 1 + c) * WP + j]));
-    atomicAdd(&e.dWL[j], acc_s[(nh + 4) * WP + j]);
+  for (int t = threadIdx.x; t < kEndsQ * 8 + 1; t += blockDim.x) {
+    float v = 0.f;
+    for (int w = 0; w < kEndsWarps; ++w) v += part[w][t];
+    if (t == kEndsQ * 8) {
+      if (f8 == 0) atomicAdd(e.dbL, v);
+      continue;
+    }
+    const int qq = t >> 3, j = f8 * 8 + (t & 7);
+    if (qq <= 2) {
+      if (qq <= nh) atomicAdd(&e.db[qq][j], __fmul_rn(e.omega[qq], v));
+    } else if (qq <= 5) {
+      atomicAdd(&e.dW0[j * 3 + (qq - 3)], __fmul_rn(e.omega[0], v));
+    } else {
+      atomicAdd(&e.dWL[j], v);
+    }
   }
-  if (threadIdx.x == 0) atomicAdd(e.dbL, acc_s[nq * WP]);
 }
 
 template <int WP, int STAGES, int U>
@@ -930,11 +921,11 @@ extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const fl
   e.dW0 = dW[0];
   e.dWL = dW[L - 1];
   e.dbL = db[L - 1];
-  const int nq = (nh + 1) + 3 + 1;
-  const size_t esmem = ((size_t)nq * WP + 1) * sizeof(float);
-  int64_t eb = 2 * (int64_t)sm_count();
-  if (eb > e.nblocks) eb = e.nblocks;
-  train_tc_ends_kernel<<<(unsigned)eb, 256, esmem, s>>>(e);
+  int64_t splits = (4 * (int64_t)sm_count()) / (WP / 8);
+  const int64_t wmax = (e.nblocks + kEndsWarps - 1) / kEndsWarps;
+  if (splits > wmax) splits = wmax;
+  if (splits < 1) splits = 1;
+  train_tc_ends_kernel<<<dim3((unsigned)(WP / 8), (unsigned)splits), kEndsWarps * 32, 0, s>>>(e);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }
