@@ -447,9 +447,15 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
               __syncwarp();
               if (lane == 0) mbar_arrive(&achunk[c]);
             } else {
+              const float4* wo4 = reinterpret_cast<const float4*>(wout + j0);
 #pragma unroll
-              for (int jj = 0; jj < U; ++jj)
-                part = __fmaf_rn(bf16::sin_fast(__uint_as_float(r[jj])), wout[j0 + jj], part);
+              for (int j4 = 0; j4 < U / 4; ++j4) {
+                const float4 wv = wo4[j4];
+                const float wa[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                  part = __fmaf_rn(bf16::sin_fast(__uint_as_float(r[4 * j4 + i])), wa[i], part);
+              }
               if (c < NCn) {
                 bf16::layer0_unit<T, false, U>(sA, w0n, m, j0, 0, 0.f, xn, yn, zn);
                 fence_proxy_async_smem();

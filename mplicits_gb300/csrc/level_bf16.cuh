@@ -83,11 +83,11 @@ struct Bf16Cfg {
 // sin through the hardware approximation.  The unit reduces its argument
 // itself after a float32 multiply by 1/(2 pi), so for the phases of these
 // networks (|z| <~ 60) the absolute error stays near 1e-6, three orders below
-// the BF16 rounding of the activations it feeds.  `phase` is 0, or pi/2 for
-// a cosine.
-__device__ __forceinline__ float sin_fast(float z, float phase = 0.f) {
-  return __sinf(z + phase);
-}
+// the BF16 rounding of the activations it feeds.  The two-argument form adds
+// `phase` first (pi/2 for a cosine); the one-argument form has no add, since
+// z + 0.f cannot be folded away (it turns -0 into +0).
+__device__ __forceinline__ float sin_fast(float z) { return __sinf(z); }
+__device__ __forceinline__ float sin_fast(float z, float phase) { return __sinf(z + phase); }
 
 // Bounded wait: the thread sleeps in hardware between polls (up to 20 us a
 // poll), leaves early when another role raised the abort flag, and gives up
@@ -420,10 +420,17 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
               __syncwarp();
               if (lane == 0) mbar_arrive(&achunk[c]);
             } else {
+              const float4* wo4 = reinterpret_cast<const float4*>(wout + j0);
 #pragma unroll
-              for (int jj = 0; jj < U; ++jj) {
-                const float sv = GRAD ? __uint_as_float(r[jj]) : sin_fast(__uint_as_float(r[jj]));
-                part = __fmaf_rn(sv, wout[j0 + jj], part);
+              for (int j4 = 0; j4 < U / 4; ++j4) {
+                const float4 wv = wo4[j4];
+                const float wa[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                  const float acc = __uint_as_float(r[4 * j4 + i]);
+                  const float sv = GRAD ? acc : sin_fast(acc);
+                  part = __fmaf_rn(sv, wa[i], part);
+                }
               }
               if (has_next) {
                 layer0_unit<T, GRAD, U>(sA, w0f, m, j0, ch, phase, xn, yn, zn);
