@@ -375,9 +375,13 @@ int mpl_batch_autotune(const MplBatchPlan* plan, int32_t repeats, MplBatchConfig
 
 /* Process-wide kernel options (read at each launch). */
 enum {
-  MPL_OPT_BF16_EPILOGUE_UNIT = 1 /* features per epilogue warp and 64-wide chunk of
-                                    the BF16 level kernel: 16 (16 epilogue warps,
-                                    default) or 32 (8 warps)                     */
+  MPL_OPT_BF16_EPILOGUE_UNIT = 1, /* features per epilogue warp and 64-wide chunk of
+                                     the BF16 level kernel: 16 (16 epilogue warps,
+                                     default) or 32 (8 warps)                    */
+  MPL_OPT_TC_TILES_IN_FLIGHT = 2  /* tiles per CTA of the tensor-core level kernel:
+                                     2 (default; GEMMs of one tile overlap the
+                                     epilogue of the other, results identical) or
+                                     1 (single-tile kernel)                      */
 };
 int mpl_set_option(int32_t option, int64_t value);
 int mpl_get_option(int32_t option, int64_t* value);

@@ -83,7 +83,7 @@ struct Cfg {
   static constexpr uint32_t oA = 0;                                // bf16 [128][256]
   static constexpr uint32_t oW = kM * kWPMax * 2;                  // [S] weight chunks
   static constexpr uint32_t oSlot = oW + STAGES * kStageMax;       // [2] constants
-  // within a slot: bias tiles, then w0f (float4 [WP]), then wout (float [WP])
+  // within a slot: bias tiles, then w0f ([4][WP] floats), then wout (float [WP])
   static constexpr uint32_t sBx = 0;
   static constexpr uint32_t sW0 = kMaxHidden * kBiasTile;
   static constexpr uint32_t sWout = sW0 + kWPMax * 16;
@@ -384,9 +384,9 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
       const SlotInfo& info = *reinterpret_cast<const SlotInfo*>(sSlot + C::sInfo);
       const int64_t qi = (t - info.first_tile) * kM + m;
       if (qi < info.n) info_point(info, qi, p, x, y, z);
-      const float4* w0f = reinterpret_cast<const float4*>(sSlot + C::sW0);
+      const float* w0s = reinterpret_cast<const float*>(sSlot + C::sW0);
       for (int c = 0; c < info.WP / kKC; ++c) {
-        bf16::layer0_unit<T, false, U>(sA, w0f, m, c * kKC + h * U, 0, 0.f, x, y, z);
+        bf16::layer0_unit<T, false, U>(sA, w0s, info.WP, m, c * kKC + h * U, 0, 0.f, x, y, z);
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(&achunk[c]);
@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
       const SlotInfo& ninfo = *reinterpret_cast<const SlotInfo*>(sn + C::sInfo);
       const int nh = info.nh, NC = info.WP / kKC;
       const float* wout = reinterpret_cast<const float*>(sl + C::sWout);
-      const float4* w0n = reinterpret_cast<const float4*>(sn + C::sW0);
+      const float* w0n = reinterpret_cast<const float*>(sn + C::sW0);
       const int64_t tn = t + gridDim.x;
       const bool has_next = tn < total;
       int NCn = 0;
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
                   part = __fmaf_rn(bf16::sin_fast(__uint_as_float(r[4 * j4 + i])), wa[i], part);
               }
               if (c < NCn) {
-                bf16::layer0_unit<T, false, U>(sA, w0n, m, j0, 0, 0.f, xn, yn, zn);
+                bf16::layer0_unit<T, false, U>(sA, w0n, ninfo.WP, m, j0, 0, 0.f, xn, yn, zn);
                 fence_proxy_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&achunk[c]);
@@ -468,7 +468,8 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
         if (l == nh) {
           // a wider next entry: its remaining layer-0 chunks
           for (int c = NC; c < NCn; ++c) {
-            bf16::layer0_unit<T, false, U>(sA, w0n, m, c * kKC + h * U, 0, 0.f, xn, yn, zn);
+            bf16::layer0_unit<T, false, U>(sA, w0n, ninfo.WP, m, c * kKC + h * U, 0, 0.f, xn, yn,
+                                           zn);
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(&achunk[c]);

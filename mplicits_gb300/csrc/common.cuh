@@ -164,7 +164,7 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 //   wht_l [WP][WP]    W_l transposed (k, j)  bh_l [WP]    l = 1..L-2
 //   wout  [WP]        bout [4]
 // BF16 section (tcgen05 kernels), omega folded in:
-//   w0f   [WP][4]     (omega0*W0[j,0..2], omega0*b0[j])
+//   w0f   [4][WP]     rows omega0*W0[:,0], omega0*W0[:,1], omega0*W0[:,2], omega0*b0
 //   hb_l  [WP]        omega_l * b_l
 //   hw_l  bf16 omega_l*W_l in UMMA K-major no-swizzle core-matrix tiles,
 //         split into K chunks of 64: chunk c, row n, col k lives at

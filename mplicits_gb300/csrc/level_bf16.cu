@@ -1,6 +1,7 @@
-// Dispatch of the tensor-core level kernels (kernel template in
-// level_bf16.cuh): operand type by precision (BF16 or FP16), epilogue unit
-// width by the MPL_OPT_BF16_EPILOGUE_UNIT option.
+// Dispatch of the tensor-core level kernels (templates in level_bf16.cuh and
+// level_pp.cuh): operand type by precision (BF16 or FP16), epilogue unit
+// width by MPL_OPT_BF16_EPILOGUE_UNIT, one or two tiles in flight per CTA by
+// MPL_OPT_TC_TILES_IN_FLIGHT.
 #include "level.cuh"
 
 namespace mpl {
@@ -9,10 +10,21 @@ int launch_level_tc_u16_bf16(const LevelArgs& a, cudaStream_t s);
 int launch_level_tc_u32_bf16(const LevelArgs& a, cudaStream_t s);
 int launch_level_tc_u16_f16(const LevelArgs& a, cudaStream_t s);
 int launch_level_tc_u32_f16(const LevelArgs& a, cudaStream_t s);
+int launch_level_pp_u16_bf16(const LevelArgs& a, cudaStream_t s);
+int launch_level_pp_u32_bf16(const LevelArgs& a, cudaStream_t s);
+int launch_level_pp_u16_f16(const LevelArgs& a, cudaStream_t s);
+int launch_level_pp_u32_f16(const LevelArgs& a, cudaStream_t s);
 
 int launch_level_tc(const LevelArgs& a, bool f16, cudaStream_t s) {
   if (a.lay.nh == 0) return launch_level_fp32(a, s);  // no hidden GEMM for the tensor cores
   const bool u32 = option_value(MPL_OPT_BF16_EPILOGUE_UNIT) == 32;
+  if (option_value(MPL_OPT_TC_TILES_IN_FLIGHT) == 2) {
+    // two tiles per CTA where the level's constants fit next to two A tiles
+    int st;
+    if (f16) st = u32 ? launch_level_pp_u32_f16(a, s) : launch_level_pp_u16_f16(a, s);
+    else st = u32 ? launch_level_pp_u32_bf16(a, s) : launch_level_pp_u16_bf16(a, s);
+    if (st != MPL_ERR_UNSUPPORTED) return st;
+  }
   if (f16) return u32 ? launch_level_tc_u32_f16(a, s) : launch_level_tc_u16_f16(a, s);
   return u32 ? launch_level_tc_u32_bf16(a, s) : launch_level_tc_u16_bf16(a, s);
 }

@@ -152,23 +152,69 @@ __device__ __forceinline__ void store_a_unit(uint8_t* sA, int m, int j0, const f
   }
 }
 
+// Paired FP32 arithmetic (sm_100 family): two IEEE fma.rn in one
+// instruction, so results equal the scalar form bit for bit.
+__device__ __forceinline__ uint64_t f2pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// First-layer phases z_j = omega0 (W0 x + b0)_j of features j..j+3 for one
+// point, evaluated as fma(x, wx, fma(y, wy, fma(z, wz, wb))) two features at
+// a time.  w0s is the [4][stride] image (rows: omega0 W0[:, 0..2], omega0 b0);
+// the x, y, z weights are returned for the tangent rows.
+__device__ __forceinline__ void phase4(const float* w0s, int stride, int j, float x, float y,
+                                       float z, float (&zz)[4], float4& wx, float4& wy,
+                                       float4& wz) {
+  wx = *reinterpret_cast<const float4*>(w0s + j);
+  wy = *reinterpret_cast<const float4*>(w0s + stride + j);
+  wz = *reinterpret_cast<const float4*>(w0s + 2 * stride + j);
+  const float4 wb = *reinterpret_cast<const float4*>(w0s + 3 * stride + j);
+  const uint64_t X = f2pack(x, x), Y = f2pack(y, y), Z = f2pack(z, z);
+  const uint64_t a = ffma2(X, f2pack(wx.x, wx.y),
+                           ffma2(Y, f2pack(wy.x, wy.y), ffma2(Z, f2pack(wz.x, wz.y),
+                                                              f2pack(wb.x, wb.y))));
+  const uint64_t b = ffma2(X, f2pack(wx.z, wx.w),
+                           ffma2(Y, f2pack(wy.z, wy.w), ffma2(Z, f2pack(wz.z, wz.w),
+                                                              f2pack(wb.z, wb.w))));
+  f2unpack(a, zz[0], zz[1]);
+  f2unpack(b, zz[2], zz[3]);
+}
+
 // Layer 0 of one U-feature unit (features j0..j0+U-1) for this thread's row:
-// FP32 phase omega0*(W0 x + b0) (omega folded into w0f), sine, BF16 into the
-// A operand.  GRAD: tangent row ch gets cos(z) * omega0*W0[:, ch-1].
+// FP32 phase omega0*(W0 x + b0) (omega folded into w0s), sine, 16-bit into
+// the A operand.  GRAD: tangent row ch gets cos(z) * omega0*W0[:, ch-1].
 template <typename T, bool GRAD, int U>
-__device__ __forceinline__ void layer0_unit(uint8_t* sA, const float4* w0f, int m, int j0, int ch,
-                                            float phase, float x, float y, float z) {
+__device__ __forceinline__ void layer0_unit(uint8_t* sA, const float* w0s, int stride, int m,
+                                            int j0, int ch, float phase, float x, float y,
+                                            float z) {
   float v[U];
 #pragma unroll
-  for (int jj = 0; jj < U; ++jj) {
-    const float4 wv = w0f[j0 + jj];
-    const float zz = __fmaf_rn(x, wv.x, __fmaf_rn(y, wv.y, __fmaf_rn(z, wv.z, wv.w)));
-    if (GRAD) {
-      const float dz = ch == 1 ? wv.x : (ch == 2 ? wv.y : wv.z);
-      const float sc = sin_fast(zz, phase);
-      v[jj] = ch ? __fmul_rn(sc, dz) : sc;
-    } else {
-      v[jj] = sin_fast(zz);
+  for (int j4 = 0; j4 < U / 4; ++j4) {
+    float zz[4];
+    float4 wx, wy, wz;
+    phase4(w0s, stride, j0 + 4 * j4, x, y, z, zz, wx, wy, wz);
+    const float ax[4] = {wx.x, wx.y, wx.z, wx.w};
+    const float ay[4] = {wy.x, wy.y, wy.z, wy.w};
+    const float az[4] = {wz.x, wz.y, wz.z, wz.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (GRAD) {
+        const float dz = ch == 1 ? ax[i] : (ch == 2 ? ay[i] : az[i]);
+        const float sc = sin_fast(zz[i], phase);
+        v[4 * j4 + i] = ch ? __fmul_rn(sc, dz) : sc;
+      } else {
+        v[4 * j4 + i] = sin_fast(zz[i]);
+      }
     }
   }
   store_a_unit<T, U>(sA, m, j0, v);
@@ -191,7 +237,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem + C::oA;
   uint8_t* sW = smem + C::oW;
-  float4* w0f = reinterpret_cast<float4*>(smem + C::oW0);
+  float* w0s = reinterpret_cast<float*>(smem + C::oW0);  // [4][WP]
   float* wout = reinterpret_cast<float*>(smem + C::oWout);
   float* red = reinterpret_cast<float*>(smem + C::oRed);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::oBar);
@@ -237,7 +283,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
   {
     const float4* g0 = reinterpret_cast<const float4*>(pk + a.lay.w0f);
     for (int i = threadIdx.x; i < WP; i += kThreads) {
-      w0f[i] = g0[i];
+      reinterpret_cast<float4*>(w0s)[i] = g0[i];
       wout[i] = reinterpret_cast<const float*>(pk + a.lay.wout)[i];
     }
     for (int l = 1; l <= nh; ++l) {
@@ -361,7 +407,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
     }
 #pragma unroll 1
     for (int c = 0; c < NC; ++c) {
-      layer0_unit<T, GRAD, U>(sA, w0f, m, c * kKC + h * U, ch, phase, x, y, z);
+      layer0_unit<T, GRAD, U>(sA, w0s, WP, m, c * kKC + h * U, ch, phase, x, y, z);
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&achunk[c]);
@@ -433,7 +479,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
                 }
               }
               if (has_next) {
-                layer0_unit<T, GRAD, U>(sA, w0f, m, j0, ch, phase, xn, yn, zn);
+                layer0_unit<T, GRAD, U>(sA, w0s, WP, m, j0, ch, phase, xn, yn, zn);
                 fence_proxy_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&achunk[c]);

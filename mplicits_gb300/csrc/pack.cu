@@ -68,11 +68,11 @@ __global__ void pack_layer0(const float* __restrict__ W, const float* __restrict
   for (int c = 0; c < 3; ++c) {
     float w = v ? W[j * 3 + c] : 0.f;
     w0t[c * WP + j] = w;
-    w0f[j * 4 + c] = omega * w;
+    w0f[c * WP + j] = omega * w;
   }
   float bb = v ? b[j] : 0.f;
   b0[j] = bb;
-  w0f[j * 4 + 3] = omega * bb;
+  w0f[3 * WP + j] = omega * bb;
 }
 
 __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict__ b, int out,

@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem + C::oA;
   uint8_t* sW = smem + C::oW;
-  float4* w0f = reinterpret_cast<float4*>(smem + C::oW0);
+  float* w0s = reinterpret_cast<float*>(smem + C::oW0);  // [4][WP]
   float* wout = reinterpret_cast<float*>(smem + C::oWout);
   float* red = reinterpret_cast<float*>(smem + C::oRed);
   float* seedbuf = reinterpret_cast<float*>(smem + C::oSeed);
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
   {
     const float4* g0 = reinterpret_cast<const float4*>(pk + a.lay.w0f);
     for (int i = threadIdx.x; i < WP; i += kThreads) {
-      w0f[i] = g0[i];
+      reinterpret_cast<float4*>(w0s)[i] = g0[i];
       wout[i] = reinterpret_cast<const float*>(pk + a.lay.wout)[i];
     }
     for (int l = 1; l <= nh; ++l) {
@@ -319,12 +319,19 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
         const int j0 = c * kKC + h * U;
         float v[U];
 #pragma unroll
-        for (int jj = 0; jj < U; ++jj) {
-          const float4 wv = w0f[j0 + jj];
-          const float zz = __fmaf_rn(x, wv.x, __fmaf_rn(y, wv.y, __fmaf_rn(z, wv.z, wv.w)));
-          const float dz0 = ch == 1 ? wv.x : (ch == 2 ? wv.y : wv.z);
-          const float sc = bf16::sin_fast(zz, ch ? kHalfPi : 0.f);
-          v[jj] = ch ? __fmul_rn(sc, dz0) : sc;
+        for (int j4 = 0; j4 < U / 4; ++j4) {
+          float zz[4];
+          float4 wx, wy, wz;
+          bf16::phase4(w0s, WP, j0 + 4 * j4, x, y, z, zz, wx, wy, wz);
+          const float ax[4] = {wx.x, wx.y, wx.z, wx.w};
+          const float ay[4] = {wy.x, wy.y, wy.z, wy.w};
+          const float az[4] = {wz.x, wz.y, wz.z, wz.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float dz0 = ch == 1 ? ax[i] : (ch == 2 ? ay[i] : az[i]);
+            const float sc = bf16::sin_fast(zz[i], ch ? kHalfPi : 0.f);
+            v[4 * j4 + i] = ch ? __fmul_rn(sc, dz0) : sc;
+          }
         }
         store_unit<U>(sA, a.s_tiles, grow, m, j0, WP, v);
         fence_proxy_async_smem();
@@ -499,18 +506,28 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
             tc::wait_ld();
             float v[U];
 #pragma unroll
-            for (int jj = 0; jj < U; ++jj) {
-              const float4 wv = w0f[j0 + jj];
-              const float zv = __fmaf_rn(x, wv.x, __fmaf_rn(y, wv.y, __fmaf_rn(z, wv.z, wv.w)));
-              const float zt = ch == 1 ? wv.x : (ch == 2 ? wv.y : wv.z);
-              const float ds = __uint_as_float(dr[jj]);
-              float tt = ch ? __fmul_rn(ds, zt) : 0.f;
-              tt = __fadd_rn(tt, __shfl_xor_sync(0xffffffffu, tt, 1));
-              tt = __fadd_rn(tt, __shfl_xor_sync(0xffffffffu, tt, 2));
-              const float cv = bf16::sin_fast(zv, kHalfPi);
-              const float sv = bf16::sin_fast(zv);
-              const float dz = ch ? __fmul_rn(cv, ds) : __fsub_rn(__fmul_rn(cv, ds), __fmul_rn(sv, tt));
-              v[jj] = valid ? dz : 0.f;
+            for (int j4 = 0; j4 < U / 4; ++j4) {
+              float zq[4];
+              float4 wx, wy, wz;
+              bf16::phase4(w0s, WP, j0 + 4 * j4, x, y, z, zq, wx, wy, wz);
+              const float ax[4] = {wx.x, wx.y, wx.z, wx.w};
+              const float ay[4] = {wy.x, wy.y, wy.z, wy.w};
+              const float az[4] = {wz.x, wz.y, wz.z, wz.w};
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                const int jj = 4 * j4 + i;
+                const float zv = zq[i];
+                const float zt = ch == 1 ? ax[i] : (ch == 2 ? ay[i] : az[i]);
+                const float ds = __uint_as_float(dr[jj]);
+                float tt = ch ? __fmul_rn(ds, zt) : 0.f;
+                tt = __fadd_rn(tt, __shfl_xor_sync(0xffffffffu, tt, 1));
+                tt = __fadd_rn(tt, __shfl_xor_sync(0xffffffffu, tt, 2));
+                const float cv = bf16::sin_fast(zv, kHalfPi);
+                const float sv = bf16::sin_fast(zv);
+                const float dz =
+                    ch ? __fmul_rn(cv, ds) : __fsub_rn(__fmul_rn(cv, ds), __fmul_rn(sv, tt));
+                v[jj] = valid ? dz : 0.f;
+              }
             }
             store_unit<U>(nullptr, dg, grow, m, j0, WP, v);
           }

@@ -124,3 +124,30 @@ def test_fp16_operands_meet_the_error_target_on_trained_levels(lib):
         out = level_forward(m, torch.from_numpy(x).cuda()).cpu().numpy()
         ref = siren.siren_forward(params, m.omegas(), x, np.float64)
         assert np.abs(out - ref).max() <= 5e-4, i
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("cfg", [[256, 256, 256], [128, 128, 128], [64, 64], [100, 60, 17],
+                                 [256, 256, 256, 256, 256]])
+@pytest.mark.parametrize("P", [1, 129, 777, 40000])
+def test_two_tile_kernel_equals_single_tile_kernel(lib, epilogue_unit, cfg, P, prec):
+    """The two-tiles-per-CTA kernel computes every element with the single-
+    tile kernel's arithmetic: values, gradients and band lists are identical."""
+    from mplicits_gb300 import capi
+    from mplicits_gb300.grad import level_gradient
+    from mplicits_gb300.model import level_forward
+    m, _ = _model(cfg, 11 + len(cfg))
+    rng = np.random.default_rng(P + 1)
+    x = torch.from_numpy(rng.uniform(-1, 1, (P, 3)).astype(np.float32)).cuda()
+    out = {}
+    for tiles in (1, 2):
+        capi.set_option(capi.MPL_OPT_TC_TILES_IN_FLIGHT, tiles)
+        try:
+            S = level_forward(m, x, precision=prec).clone()
+            Sg, G = level_gradient(m, x, precision=prec)
+            out[tiles] = (S, Sg.clone(), G.clone())
+        finally:
+            capi.set_option(capi.MPL_OPT_TC_TILES_IN_FLIGHT, 2)
+    for a, b in zip(out[1], out[2]):
+        assert torch.equal(a, b)
+    assert capi.device_status() == capi.MPL_OK
