@@ -708,10 +708,13 @@ def main():
     peak_tf, hbm, src = peaks()
     achieved_tf = FLOP_PER_POINT * N ** 3 / (l0_ms * 1e-3) / 1e12
     traffic = None
+    kernel_name = "level 0 tensor-core launch"
     prof = os.path.join(ROOT, "profiles", "level_bf16_512.json")
     if os.path.exists(prof):
         with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            pj = json.load(f)
+        traffic = pj.get("dram_bytes_per_launch")
+        kernel_name = pj.get("kernel", kernel_name)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -744,7 +747,7 @@ def main():
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "mplicits_gb300.meshing.BandedReconstruction.sample()+mesh() with "
                             "weights copied from pinned host memory and the mesh copied back"},
-            "roofline": {"bound": "tensor", "kernel": "level_bf16_kernel<256> (level 0, full grid)",
+            "roofline": {"bound": "tensor", "kernel": kernel_name + " (level 0, full grid)",
                          "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
                          "frac": achieved_tf / peak_tf, "peak_source": f"{src} bf16 sustained",
                          "flop_per_point": FLOP_PER_POINT, "points_per_launch": N ** 3,
