@@ -242,17 +242,30 @@ int mpl_train_scratch_floats(const MplNet* net, int64_t n, int64_t* floats);
 int mpl_train_forward(const MplNet* net, const void* packed_dev, const float* xyz_dev, int64_t n,
                       float* S_dev, float* G_dev, float* pre_dev, void* stream);
 
-/* The residual-level loss of the reference's fine trainer on n points
- * (loss_add_detail_fine): with S = f + f_frozen and G = g + g_frozen,
- * sdf (gt - S)^2 and normal 1 - cos(n_gt, G) where gt_sdf != -1, eikonal
- * (|G| - 1)^2 everywhere.  Writes the three sums to loss_sums[3] (divide by
- * n and weight as the reference does) and the derivative seeds
- * seeds [n, 4] = (dL/df, dL/dG) of the weighted mean loss.  f_frozen and
- * g_frozen are nullable (no frozen levels). */
+/* Loss of a training step. */
+enum {
+  MPL_LOSS_RESIDUAL = 0, /* loss_add_detail(_fine), i3d/loss_functions.py:263-394:
+                            weight = {sdf, normal, eikonal, -}; S and G include
+                            the frozen levels' sums; gt == -1 marks points
+                            without SDF and normal supervision               */
+  MPL_LOSS_TRUE_SDF = 1  /* true_sdf, i3d/loss_functions.py:123-163 (the coarse
+                            trainer): weight = {sdf on surface, sdf off surface,
+                            normal, eikonal}; gt == 0 marks surface points     */
+};
+
+typedef struct MplLoss {
+  int32_t kind;
+  float weight[4];
+} MplLoss;
+
+/* A trainer's loss on n points with S = f + f_frozen and G = g + g_frozen
+ * (f_frozen, g_frozen nullable): the per-term sums over the points into
+ * loss_sums[4] (divide by n and weight as the reference does; the residual
+ * loss has three terms, the fourth sum is 0) and the derivative seeds
+ * seeds [n, 4] = (dL/df, dL/dG) of the weighted mean loss. */
 int mpl_train_loss(int64_t n, const float* f_dev, const float* g_dev, const float* f_frozen_dev,
                    const float* g_frozen_dev, const float* gt_sdf_dev, const float* gt_normals_dev,
-                   float w_sdf, float w_normal, float w_eikonal, float* seeds_dev,
-                   float* loss_sums_dev, void* stream);
+                   const MplLoss* loss, float* seeds_dev, float* loss_sums_dev, void* stream);
 
 /* Weight gradients of a loss given its seeds on (f, df/dx) of every point:
  * the backward through the level's forward-mode graph (double backward of
@@ -272,21 +285,20 @@ int mpl_train_tc_scratch_bytes(const MplNet* net, int64_t n, int64_t* bytes);
 
 /* The training step of one level on the tensor cores (BF16 operands, FP32
  * accumulation, FP32 master weights outside): forward in forward mode, the
- * residual loss of the fine trainer with S = f + f_frozen and
- * G = df/dx + g_frozen (as mpl_train_loss, sums into loss_sums[3], seeds
- * [n, 4] written, 16-byte aligned), the backward through the forward-mode
- * graph (double backward included) and every weight gradient, ADDED into
- * the padded buffers dW[l] / db[l] of mpl_train_backward.  Replaces the
- * reference trainer's forward, loss_add_detail_fine and loss.backward()
- * (experiment_scripts/train_sdf_on_neighborhood_fine.py:247-250,
- * i3d/loss_functions.py:347-394).  Levels with 1 or 2 hidden GEMMs of padded
- * width 128 or 256. */
+ * loss with S = f + f_frozen and G = df/dx + g_frozen (as mpl_train_loss:
+ * sums into loss_sums[4], seeds [n, 4] written, 16-byte aligned), the
+ * backward through the forward-mode graph (double backward included) and
+ * every weight gradient, ADDED into the padded buffers dW[l] / db[l] of
+ * mpl_train_backward.  Replaces the reference trainers' forward, loss and
+ * loss.backward() (experiment_scripts/train_sdf_on_neighborhood_fine.py:
+ * 247-250 with i3d/loss_functions.py:347-394; the coarse trainer with
+ * true_sdf).  Levels with 1 or 2 hidden GEMMs of padded width 128 or 256. */
 int mpl_train_tc_step(const MplNet* net, const void* packed_dev, const float* xyz_dev, int64_t n,
                       const float* f_frozen_dev, const float* g_frozen_dev,
-                      const float* gt_sdf_dev, const float* gt_normals_dev, float w_sdf,
-                      float w_normal, float w_eikonal, void* scratch_dev, int64_t scratch_bytes,
-                      float* seeds_dev, float* loss_sums_dev, float* const* dW_dev,
-                      float* const* db_dev, void* stream);
+                      const float* gt_sdf_dev, const float* gt_normals_dev, const MplLoss* loss,
+                      void* scratch_dev, int64_t scratch_bytes, float* seeds_dev,
+                      float* loss_sums_dev, float* const* dW_dev, float* const* db_dev,
+                      void* stream);
 
 /* Flags of mpl_train_batch. */
 #define MPL_BATCH_NEIGH_DELTA 1 /* offset scale from the last column (use_neigh_delta) */

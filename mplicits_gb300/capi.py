@@ -69,6 +69,15 @@ class MplCamera(ctypes.Structure):
                 ("height", ctypes.c_int32)]
 
 
+class MplLoss(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32),
+                ("weight", ctypes.c_float * 4)]
+
+
+MPL_LOSS_RESIDUAL = 0
+MPL_LOSS_TRUE_SDF = 1
+
+
 class MplBatchEntry(ctypes.Structure):
     _fields_ = [("net", MplNet),
                 ("packed_dev", ctypes.c_void_p),
@@ -125,13 +134,14 @@ SIGNATURES = {
     "mpl_train_scratch_floats": (ctypes.c_int, [ctypes.POINTER(MplNet), _I64,
                                                 ctypes.POINTER(_I64)]),
     "mpl_train_forward": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _P, _I64, _P, _P, _P, _P]),
-    "mpl_train_loss": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P, _P, _F, _F, _F, _P, _P, _P]),
+    "mpl_train_loss": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P, _P, ctypes.POINTER(MplLoss), _P,
+                                      _P, _P]),
     "mpl_train_backward": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _P, _I64, _P, _P, _P, _P,
                                           _P, _P]),
     "mpl_train_tc_scratch_bytes": (ctypes.c_int, [ctypes.POINTER(MplNet), _I64,
                                                   ctypes.POINTER(_I64)]),
     "mpl_train_tc_step": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _P, _I64, _P, _P, _P, _P,
-                                         _F, _F, _F, _P, _I64, _P, _P, _P, _P, _P]),
+                                         ctypes.POINTER(MplLoss), _P, _I64, _P, _P, _P, _P, _P]),
     "mpl_train_batch": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _F, _F, _I32,
                                        ctypes.c_uint64, _P, _P, _P, _P]),
     "mpl_adam_step": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _F, _F, _F, _F, _I64, _P]),

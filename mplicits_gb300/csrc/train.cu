@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include "level.cuh"
+#include "train_loss.cuh"
 
 namespace mpl {
 
@@ -305,59 +306,31 @@ __global__ void __launch_bounds__(256) train_wgrad_ends_kernel(const TrainArgs a
   }
 }
 
-// Loss of the residual trainer (i3d/loss_functions.py:347-394) per point and
-// its derivative seeds w.r.t. this level's f and df/dx.  S = f + F (frozen
-// levels), G = g + Gf.  Sums: loss[0] sdf, [1] normal, [2] eikonal.
+// The trainers' losses per point (train_loss.cuh) and their seeds; the four
+// term sums per block are added atomically.
 __global__ void train_loss_kernel(int64_t n, const float* __restrict__ f, const float* __restrict__ g,
                                   const float* __restrict__ Ff, const float* __restrict__ Gf,
                                   const float* __restrict__ gt_sdf,
-                                  const float* __restrict__ gt_n, float w_sdf, float w_normal,
-                                  float w_eik, float* __restrict__ seed, float* __restrict__ loss) {
+                                  const float* __restrict__ gt_n, const LossParams L,
+                                  float* __restrict__ seed, float* __restrict__ loss) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  float l_sdf = 0.f, l_n = 0.f, l_e = 0.f;
+  float term[4] = {0.f, 0.f, 0.f, 0.f};
   if (q < n) {
-    const float inv_n = 1.0f / (float)n;
     const float S = __fadd_rn(f[q], Ff ? Ff[q] : 0.f);
     float G[3], N[3];
     for (int c = 0; c < 3; ++c) {
       G[c] = __fadd_rn(g[3 * q + c], Gf ? Gf[3 * q + c] : 0.f);
       N[c] = gt_n[3 * q + c];
     }
-    const bool sup = gt_sdf[q] != -1.0f;
-    float phi = 0.f, gam[3] = {0.f, 0.f, 0.f};
-    const float gl = sqrtf(G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
-    if (sup) {
-      const float r = __fsub_rn(gt_sdf[q], S);
-      l_sdf = r * r;
-      phi = -2.0f * r * w_sdf * inv_n;
-      const float nl = sqrtf(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
-      const float nn = fmaxf(nl, 1e-8f), gg = fmaxf(gl, 1e-8f);
-      const float dot = N[0] * G[0] + N[1] * G[1] + N[2] * G[2];
-      const float cosv = dot / (nn * gg);
-      l_n = 1.0f - cosv;
-      // d(1 - cos)/dG = -(N / (nn gg) - cos G / gg^2) (gl > eps)
-      const float sc = w_normal * inv_n;
-      for (int c = 0; c < 3; ++c) gam[c] -= sc * (N[c] / (nn * gg) - (gl > 1e-8f ? cosv * G[c] / (gg * gg) : 0.f));
-    }
-    const float ge = gl - 1.0f;
-    l_e = ge * ge;
-    if (gl > 0.f) {
-      const float sc = 2.0f * ge * w_eik * inv_n / gl;
-      for (int c = 0; c < 3; ++c) gam[c] += sc * G[c];
-    }
+    float phi, gam[3];
+    point_loss(L, S, G, gt_sdf[q], N, phi, gam, term);
     seed[4 * q] = phi;
     for (int c = 0; c < 3; ++c) seed[4 * q + 1 + c] = gam[c];
   }
-  // block reduction of the three sums
-  for (int o = 16; o >= 1; o >>= 1) {
-    l_sdf += __shfl_xor_sync(0xffffffffu, l_sdf, o);
-    l_n += __shfl_xor_sync(0xffffffffu, l_n, o);
-    l_e += __shfl_xor_sync(0xffffffffu, l_e, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&loss[0], l_sdf);
-    atomicAdd(&loss[1], l_n);
-    atomicAdd(&loss[2], l_e);
+  for (int k = 0; k < 4; ++k) {
+    float v = term[k];
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(&loss[k], v);
   }
 }
 
@@ -512,14 +485,16 @@ extern "C" int mpl_train_forward(const MplNet* net, const void* packed, const fl
 
 extern "C" int mpl_train_loss(int64_t n, const float* f, const float* g, const float* f_frozen,
                               const float* g_frozen, const float* gt_sdf, const float* gt_normals,
-                              float w_sdf, float w_normal, float w_eikonal, float* seeds,
-                              float* loss_sums, void* stream) {
+                              const MplLoss* loss, float* seeds, float* loss_sums, void* stream) {
   if (!f || !g || !gt_sdf || !gt_normals || !seeds || !loss_sums || n < 0) return MPL_ERR_INVALID_ARG;
+  LossParams L;
+  int st = loss_params(loss, n, &L);
+  if (st != MPL_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  MPL_CUDA_TRY(cudaMemsetAsync(loss_sums, 0, 3 * sizeof(float), s));
+  MPL_CUDA_TRY(cudaMemsetAsync(loss_sums, 0, 4 * sizeof(float), s));
   if (n == 0) return MPL_OK;
   train_loss_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-      n, f, g, f_frozen, g_frozen, gt_sdf, gt_normals, w_sdf, w_normal, w_eikonal, seeds, loss_sums);
+      n, f, g, f_frozen, g_frozen, gt_sdf, gt_normals, L, seeds, loss_sums);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }

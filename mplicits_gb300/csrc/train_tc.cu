@@ -29,6 +29,7 @@
 #include <string.h>
 
 #include "level_bf16.cuh"
+#include "train_loss.cuh"
 
 namespace mpl {
 namespace ttc {
@@ -54,11 +55,11 @@ struct Args {
   const float* Gf;     // nullable [n][3]
   const float* gt_sdf;
   const float* gt_n;
-  float w_sdf, w_normal, w_eik, inv_n;
+  LossParams L;
   __nv_bfloat16* s_tiles;   // [nh + 1][rows_pad * WP]
   __nv_bfloat16* dz_tiles;  // [nh + 1][rows_pad * WP]
   float* seeds;             // [n][4]
-  float* loss;              // [3]
+  float* loss;              // [4]
   int64_t rows_pad;
   int* status;
 };
@@ -299,7 +300,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
     const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
     const int64_t lstride = a.rows_pad * WP;  // elements per layer in the tile buffers
     int64_t g = 0;
-    float l_sdf = 0.f, l_nrm = 0.f, l_eik = 0.f;
+    float lsum[4] = {0.f, 0.f, 0.f, 0.f};
     bool fail = false;
     float x = 0.f, y = 0.f, z = 0.f;
     bool valid = false;
@@ -401,34 +402,17 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
         float phi = 0.f, gam0 = 0.f, gam1 = 0.f, gam2 = 0.f;
         if (valid && ch == 0) {
           const float Sv = __fadd_rn(f, a.Ff ? a.Ff[qp] : 0.f);
-          const float G0 = __fadd_rn(gx, a.Gf ? a.Gf[3 * qp + 0] : 0.f);
-          const float G1 = __fadd_rn(gy, a.Gf ? a.Gf[3 * qp + 1] : 0.f);
-          const float G2 = __fadd_rn(gz, a.Gf ? a.Gf[3 * qp + 2] : 0.f);
-          const float N0 = a.gt_n[3 * qp + 0], N1 = a.gt_n[3 * qp + 1], N2 = a.gt_n[3 * qp + 2];
-          const float gt = a.gt_sdf[qp];
-          const float gl = sqrtf(G0 * G0 + G1 * G1 + G2 * G2);
-          if (gt != -1.0f) {
-            const float r = __fsub_rn(gt, Sv);
-            l_sdf += r * r;
-            phi = -2.0f * r * a.w_sdf * a.inv_n;
-            const float nl = sqrtf(N0 * N0 + N1 * N1 + N2 * N2);
-            const float nn = fmaxf(nl, 1e-8f), gg = fmaxf(gl, 1e-8f);
-            const float cosv = (N0 * G0 + N1 * G1 + N2 * G2) / (nn * gg);
-            l_nrm += 1.0f - cosv;
-            const float sc = a.w_normal * a.inv_n;
-            const float cg = gl > 1e-8f ? cosv / (gg * gg) : 0.f;
-            gam0 -= sc * (N0 / (nn * gg) - cg * G0);
-            gam1 -= sc * (N1 / (nn * gg) - cg * G1);
-            gam2 -= sc * (N2 / (nn * gg) - cg * G2);
-          }
-          const float ge = gl - 1.0f;
-          l_eik += ge * ge;
-          if (gl > 0.f) {
-            const float sc = 2.0f * ge * a.w_eik * a.inv_n / gl;
-            gam0 += sc * G0;
-            gam1 += sc * G1;
-            gam2 += sc * G2;
-          }
+          const float G[3] = {__fadd_rn(gx, a.Gf ? a.Gf[3 * qp + 0] : 0.f),
+                              __fadd_rn(gy, a.Gf ? a.Gf[3 * qp + 1] : 0.f),
+                              __fadd_rn(gz, a.Gf ? a.Gf[3 * qp + 2] : 0.f)};
+          const float N[3] = {a.gt_n[3 * qp + 0], a.gt_n[3 * qp + 1], a.gt_n[3 * qp + 2]};
+          float gam[3], term[4];
+          point_loss(a.L, Sv, G, a.gt_sdf[qp], N, phi, gam, term);
+          gam0 = gam[0];
+          gam1 = gam[1];
+          gam2 = gam[2];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) lsum[k] += term[k];
           *reinterpret_cast<float4*>(a.seeds + 4 * qp) = make_float4(phi, gam0, gam1, gam2);
         }
         const float s_phi = __shfl_sync(0xffffffffu, phi, vlane);
@@ -543,15 +527,11 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
     // loss sums of this CTA
     if (h == 0) {
 #pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) {
-        l_sdf += __shfl_xor_sync(0xffffffffu, l_sdf, o);
-        l_nrm += __shfl_xor_sync(0xffffffffu, l_nrm, o);
-        l_eik += __shfl_xor_sync(0xffffffffu, l_eik, o);
-      }
-      if (lane == 0) {
-        atomicAdd(&a.loss[0], l_sdf);
-        atomicAdd(&a.loss[1], l_nrm);
-        atomicAdd(&a.loss[2], l_eik);
+      for (int k = 0; k < 4; ++k) {
+        float v = lsum[k];
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.f) atomicAdd(&a.loss[k], v);
       }
     }
   }
@@ -861,8 +841,8 @@ extern "C" int mpl_train_tc_scratch_bytes(const MplNet* net, int64_t n, int64_t*
 
 extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const float* xyz,
                                  int64_t n, const float* f_frozen, const float* g_frozen,
-                                 const float* gt_sdf, const float* gt_normals, float w_sdf,
-                                 float w_normal, float w_eikonal, void* scratch,
+                                 const float* gt_sdf, const float* gt_normals,
+                                 const MplLoss* loss, void* scratch,
                                  int64_t scratch_bytes, float* seeds, float* loss_sums,
                                  float* const* dW, float* const* db, void* stream) {
   if (!net || !packed || !gt_sdf || !gt_normals || !seeds || !loss_sums || !dW || !db || n < 0 ||
@@ -875,6 +855,8 @@ extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const fl
   memset(&a, 0, sizeof(a));
   int st = make_layout(net, &a.lay);
   if (st != MPL_OK) return st;
+  st = loss_params(loss, n, &a.L);
+  if (st != MPL_OK) return st;
   const int nh = a.lay.nh, WP = a.lay.WP, L = a.lay.L;
   if (nh < 1 || nh > 2 || (WP != 128 && WP != 256)) return MPL_ERR_UNSUPPORTED;
   for (int l = 0; l < L; ++l)
@@ -883,7 +865,7 @@ extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const fl
   mpl_train_tc_scratch_bytes(net, n, &need);
   if (scratch_bytes < need) return MPL_ERR_CAPACITY;
   cudaStream_t s = (cudaStream_t)stream;
-  MPL_CUDA_TRY(cudaMemsetAsync(loss_sums, 0, 3 * sizeof(float), s));
+  MPL_CUDA_TRY(cudaMemsetAsync(loss_sums, 0, 4 * sizeof(float), s));
   if (n == 0) return MPL_OK;
   const int64_t rows_pad = tc_rows_pad(n);
   const int64_t lstride = rows_pad * WP;
@@ -894,10 +876,6 @@ extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const fl
   a.Gf = g_frozen;
   a.gt_sdf = gt_sdf;
   a.gt_n = gt_normals;
-  a.w_sdf = w_sdf;
-  a.w_normal = w_normal;
-  a.w_eik = w_eikonal;
-  a.inv_n = 1.0f / (float)n;
   a.s_tiles = (__nv_bfloat16*)scratch;
   a.dz_tiles = a.s_tiles + (int64_t)(nh + 1) * lstride;
   a.seeds = seeds;

@@ -25,6 +25,10 @@ from . import capi
 from .grad import level_gradient
 
 DEFAULT_WEIGHTS = {"sdf_constraint": 3e3, "normal_constraint": 1e2, "grad_constraint": 5e1}
+TRUE_SDF_WEIGHTS = {"sdf_on_surf": 3e3, "sdf_off_surf": 2e2, "normal_constraint": 1e2,
+                    "grad_constraint": 5e1}
+LOSSES = {"residual": (capi.MPL_LOSS_RESIDUAL, DEFAULT_WEIGHTS),
+          "true_sdf": (capi.MPL_LOSS_TRUE_SDF, TRUE_SDF_WEIGHTS)}
 
 
 class _Scratch:
@@ -202,34 +206,49 @@ def create_training_data_on_neighborhood(vertices, n_on_surf, device="cuda", del
 class ResidualTrainer:
     """Adam training of one level against frozen coarser levels.
 
-    ``step(x, normals, sdf)`` takes a batch built like
-    create_training_data_on_neighborhood (sdf == -1 marks points without SDF
-    or normal supervision) and returns the three weighted loss terms as a
-    device tensor [3] (sdf, normal, eikonal), without a host sync.
+    ``loss="residual"`` is the medium and fine trainers' loss_add_detail(_fine)
+    (i3d/loss_functions.py:263-394): ``step(x, normals, sdf)`` takes a batch
+    built like create_training_data_on_neighborhood (sdf == -1 marks points
+    without SDF or normal supervision) and returns the weighted terms
+    (sdf, normal, eikonal) as a device tensor [3].  ``loss="true_sdf"`` is the
+    coarse trainer's loss (i3d/loss_functions.py:123-163; no frozen levels;
+    sdf == 0 marks surface points) with terms (sdf on surface, sdf off
+    surface, normal, eikonal) [4].  No host sync either way.
     """
 
     def __init__(self, model, frozen=(), lr=1e-4, betas=(0.9, 0.999), eps=1e-8,
-                 constraint_weights=None, precision="fp32"):
+                 constraint_weights=None, precision="fp32", loss="residual"):
         if precision not in ("fp32", "bf16"):
             raise ValueError("precision is 'fp32' (plain kernels) or 'bf16' (tensor cores)")
+        if loss not in LOSSES:
+            raise ValueError(f"loss is one of {sorted(LOSSES)}")
+        if loss == "true_sdf" and frozen:
+            raise ValueError("the true_sdf loss trains a first level: no frozen levels")
         self.precision = precision
         self.model = model
         self.frozen = list(frozen)
         self.lr, self.betas, self.eps = lr, betas, eps
-        w = dict(DEFAULT_WEIGHTS)
+        kind, defaults = LOSSES[loss]
+        w = dict(defaults)
         if constraint_weights:
             w.update({k: float(v) for k, v in constraint_weights.items()})
         self.weights = w
+        self.names = list(defaults)
+        self.loss = capi.MplLoss(kind=kind)
+        for i, k in enumerate(self.names):
+            self.loss.weight[i] = w[k]
         self.params = list(model.parameters())
         self.exp_avg = [torch.zeros_like(p) for p in self.params]
         self.exp_avg_sq = [torch.zeros_like(p) for p in self.params]
         self.t = 0
-        self.loss_sums = torch.zeros(3, dtype=torch.float32, device=self.params[0].device)
+        self.loss_sums = torch.zeros(4, dtype=torch.float32, device=self.params[0].device)
+        self._scale = torch.tensor([w[k] for k in self.names], dtype=torch.float32,
+                                   device=self.params[0].device)
 
     @torch.no_grad()
     def loss_and_grads(self, x, normals, sdf):
-        """The weighted loss terms [3] (sdf, normal, eikonal) and the
-        gradients of their sum, in ``model.parameters()`` order."""
+        """The weighted loss terms (``self.names``) and the gradients of their
+        sum, in ``model.parameters()`` order."""
         x = x.detach().float().reshape(-1, 3).contiguous()
         normals = normals.detach().float().reshape(-1, 3).contiguous()
         sdf = sdf.detach().float().reshape(-1).contiguous()
@@ -244,16 +263,13 @@ class ResidualTrainer:
             return self._tc_loss_and_grads(x, normals, sdf, Ff, Gf)
         sc = _scratch(self.model, n, x.device)
         _forward_with_scratch(self.model, x, sc)
-        w = self.weights
         capi.check(capi.load().mpl_train_loss(
             n, capi.ptr(sc.f), capi.ptr(sc.g), capi.ptr(Ff), capi.ptr(Gf), capi.ptr(sdf),
-            capi.ptr(normals), w["sdf_constraint"], w["normal_constraint"], w["grad_constraint"],
-            capi.ptr(sc.seeds[:n]), capi.ptr(self.loss_sums), capi.stream_ptr()), "mpl_train_loss")
+            capi.ptr(normals), ctypes.byref(self.loss), capi.ptr(sc.seeds[:n]),
+            capi.ptr(self.loss_sums), capi.stream_ptr()), "mpl_train_loss")
         _backward(self.model, x, sc)
         grads = _unpad(self.model, sc)
-        scale = torch.tensor([w["sdf_constraint"], w["normal_constraint"], w["grad_constraint"]],
-                             dtype=torch.float32, device=x.device) / n
-        return self.loss_sums * scale, grads
+        return self.loss_sums[:len(self.names)] * (self._scale / n), grads
 
     def _tc_loss_and_grads(self, x, normals, sdf, Ff, Gf):
         """One mpl_train_tc_step: forward, loss, backward and weight gradients
@@ -279,17 +295,13 @@ class ResidualTrainer:
         P = ctypes.c_void_p
         dW = (P * len(sc.dW))(*[t.data_ptr() for t in sc.dW])
         db = (P * len(sc.db))(*[t.data_ptr() for t in sc.db])
-        w = self.weights
         capi.check(lib.mpl_train_tc_step(
             ctypes.byref(net), capi.ptr(packed), capi.ptr(x), n, capi.ptr(Ff), capi.ptr(Gf),
-            capi.ptr(sdf), capi.ptr(normals), w["sdf_constraint"], w["normal_constraint"],
-            w["grad_constraint"], ctypes.c_void_p(buf.data_ptr() + off), nb.value,
-            capi.ptr(seeds), capi.ptr(self.loss_sums), dW, db, capi.stream_ptr()),
-            "mpl_train_tc_step")
+            capi.ptr(sdf), capi.ptr(normals), ctypes.byref(self.loss),
+            ctypes.c_void_p(buf.data_ptr() + off), nb.value, capi.ptr(seeds),
+            capi.ptr(self.loss_sums), dW, db, capi.stream_ptr()), "mpl_train_tc_step")
         grads = _unpad(self.model, sc)
-        scale = torch.tensor([w["sdf_constraint"], w["normal_constraint"], w["grad_constraint"]],
-                             dtype=torch.float32, device=x.device) / n
-        return self.loss_sums * scale, grads
+        return self.loss_sums[:len(self.names)] * (self._scale / n), grads
 
     @torch.no_grad()
     def step(self, x, normals, sdf):

@@ -20,6 +20,8 @@ from __future__ import annotations
 import numpy as np
 
 DEFAULT_WEIGHTS = {"sdf_constraint": 3e3, "normal_constraint": 1e2, "grad_constraint": 5e1}
+TRUE_SDF_WEIGHTS = {"sdf_on_surf": 3e3, "sdf_off_surf": 2e2, "normal_constraint": 1e2,
+                    "grad_constraint": 5e1}
 
 
 def forward_tangent(params, omegas, x):
@@ -78,6 +80,52 @@ def residual_loss_seeds(f, g, F_frozen, G_frozen, gt_sdf, gt_normals, weights=No
     gam = gam + np.where((gl > 0)[:, None],
                          (2.0 * (gl - 1.0) * w["grad_constraint"] / n / safe)[:, None] * G, 0.0)
     return losses, phi, gam
+
+
+def true_sdf_loss_seeds(f, g, gt_sdf, gt_normals, weights=None):
+    """The coarse trainer's loss ``true_sdf`` (i3d/loss_functions.py:123-163,
+    with sdf_constraint_on_surf, sdf_constraint_off_surf,
+    vector_aligment_on_surf and eikonal_constraint at :9-42) and its seeds:
+    pred^2 where gt == 0, (gt - pred)^2 elsewhere, 1 - cos(grad, n) where
+    gt == 0, (|grad| - 1)^2 everywhere, each a mean over all points."""
+    w = dict(TRUE_SDF_WEIGHTS)
+    if weights:
+        w.update(weights)
+    n = f.shape[0]
+    gt = np.asarray(gt_sdf, np.float64).reshape(-1)
+    N = np.asarray(gt_normals, np.float64)
+    on = gt == 0
+    l_on = np.where(on, f * f, 0.0)
+    r = gt - f
+    l_off = np.where(on, 0.0, r * r)
+    gl = np.linalg.norm(g, axis=1)
+    nn = np.maximum(np.linalg.norm(N, axis=1), 1e-8)
+    gg = np.maximum(gl, 1e-8)
+    cos = np.sum(N * g, axis=1) / (nn * gg)
+    l_n = np.where(on, 1.0 - cos, 0.0)
+    l_e = (gl - 1.0) ** 2
+    losses = {"sdf_on_surf": w["sdf_on_surf"] * l_on.mean(),
+              "sdf_off_surf": w["sdf_off_surf"] * l_off.mean(),
+              "normal_constraint": w["normal_constraint"] * l_n.mean(),
+              "grad_constraint": w["grad_constraint"] * l_e.mean()}
+    phi = np.where(on, 2.0 * f * w["sdf_on_surf"] / n, -2.0 * r * w["sdf_off_surf"] / n)
+    dcos = N / (nn * gg)[:, None] - np.where(gl > 1e-8, cos / (gg * gg), 0.0)[:, None] * g
+    gam = np.where(on[:, None], -w["normal_constraint"] / n * dcos, 0.0)
+    safe = np.where(gl > 0, gl, 1.0)
+    gam = gam + np.where((gl > 0)[:, None],
+                         (2.0 * (gl - 1.0) * w["grad_constraint"] / n / safe)[:, None] * g, 0.0)
+    return losses, phi, gam
+
+
+def true_sdf_step_grads(params, omegas, x, gt_sdf, gt_normals, weights=None):
+    f, g, _ = forward_tangent(params, omegas, x)
+    losses, phi, gam = true_sdf_loss_seeds(f, g, gt_sdf, gt_normals, weights)
+    return losses, param_grads(params, omegas, x, phi, gam)
+
+
+def true_sdf_loss_total(params, omegas, x, gt_sdf, gt_normals, weights=None):
+    f, g, _ = forward_tangent(params, omegas, x)
+    return sum(true_sdf_loss_seeds(f, g, gt_sdf, gt_normals, weights)[0].values())
 
 
 def param_grads(params, omegas, x, phi, gam):

@@ -284,3 +284,25 @@ def test_batch_device_generator(lib):
     assert np.allclose(off, sdf[200:400, None] * nrm[:200], atol=1e-7)
     dith = pts[400:] - pts[:200] - 0.005 * nrm[:200]
     assert np.all((dith >= -1e-6) & (dith < 0.01 + 1e-6))
+
+
+def test_true_sdf_trainer_matches_reference_autograd(lib):
+    """The coarse trainer's loss (true_sdf) on the plain kernels against the
+    reference's own loss values and p.grad (golden loss_true_sdf.npz)."""
+    from mplicits_gb300.train import ResidualTrainer
+    d = golden("loss_true_sdf.npz")
+    sd = {k[6:]: d[k] for k in d.files if k.startswith("model.")}
+    model = _siren(sd, [32, 32, 32])
+    tr = ResidualTrainer(model, loss="true_sdf")
+    losses, grads = tr.loss_and_grads(torch.from_numpy(d["x"]).cuda(),
+                                      torch.from_numpy(d["normals"]).cuda(),
+                                      torch.from_numpy(d["sdf"]).cuda())
+    losses = losses.cpu().numpy()
+    assert tr.names == ["sdf_on_surf", "sdf_off_surf", "normal_constraint", "grad_constraint"]
+    for i, k in enumerate(tr.names):
+        ref = float(d["loss." + k])
+        assert abs(losses[i] - ref) <= 1e-4 * abs(ref), k
+    for j in range(4):
+        gw, gb = d[f"grad.net.{j}.0.weight"], d[f"grad.net.{j}.0.bias"]
+        assert np.abs(grads[2 * j].cpu().numpy() - gw).max() <= 1e-4 * np.abs(gw).max(), j
+        assert np.abs(grads[2 * j + 1].cpu().numpy() - gb).max() <= 1e-4 * np.abs(gb).max(), j

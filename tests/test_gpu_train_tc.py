@@ -97,3 +97,30 @@ def test_tensor_core_training_descends_like_fp32(lib):
     a, b = curves["fp32"], curves["bf16"]
     assert a[-1] < a[0] and b[-1] < b[0]
     assert np.all(np.abs(a - b) <= 0.05 * np.abs(a) + 1e-3), (a, b)
+
+
+@pytest.mark.parametrize("widths,n", [([256] * 3, 2500), ([128] * 3, 999)])
+def test_tensor_core_true_sdf_step_matches_oracle(lib, widths, n):
+    """The coarse trainer's loss on the tensor-core step against the FP64
+    oracle (itself pinned to the reference's true_sdf and finite differences)."""
+    from mplicits_gb300.train import ResidualTrainer
+    params = _level(widths, 77 + n)
+    rng = np.random.default_rng(n)
+    xs = rng.uniform(-0.9, 0.9, (n, 3)).astype(np.float32)
+    nrm = (xs / np.linalg.norm(xs, axis=1, keepdims=True)).astype(np.float32)
+    sdf = rng.uniform(-0.3, 0.3, (n, 1)).astype(np.float32)
+    sdf[: n // 2] = 0.0
+    nrm[n // 2:] = 0.0  # off-surface rows carry no normal, as the reference's batches
+    X, N, D = (torch.from_numpy(a).cuda() for a in (xs, nrm, sdf))
+    ref_l, ref_g = ot.true_sdf_step_grads(params, [30.0] * len(widths), xs, sdf, nrm)
+    for prec, tol_l, tol_g in (("fp32", 1e-4, 1e-4), ("bf16", 3e-2, 3e-2)):
+        tr = ResidualTrainer(_siren(params, prec), precision=prec, loss="true_sdf")
+        losses, grads = tr.loss_and_grads(X, N, D)
+        lo = losses.cpu().numpy()
+        for i, k in enumerate(tr.names):
+            assert abs(lo[i] - ref_l[k]) <= tol_l * abs(ref_l[k]) + 1e-4, (prec, k)
+        for j in range(len(params)):
+            for t in range(2):
+                got = grads[2 * j + t].cpu().numpy().astype(np.float64)
+                ref = ref_g[j][t].reshape(got.shape)
+                assert _rel(got, ref) <= tol_g, (prec, j, t, _rel(got, ref))

@@ -83,3 +83,36 @@ def test_oracle_training_batch_matches_reference():
         assert np.array_equal(p, d[f"c{c}.pts"]), c
         assert np.array_equal(nr, d[f"c{c}.normals"]), c
         assert np.array_equal(s, d[f"c{c}.sdf"]), c
+
+
+def _true_sdf_case():
+    d = golden("loss_true_sdf.npz")
+    params = [(d[f"model.net.{j}.0.weight"], d[f"model.net.{j}.0.bias"]) for j in range(4)]
+    return d, params, [30.0, 30.0, 30.0]
+
+
+def test_oracle_true_sdf_matches_reference_autograd():
+    d, params, om = _true_sdf_case()
+    losses, grads = ot.true_sdf_step_grads(params, om, d["x"], d["sdf"], d["normals"])
+    for k, v in losses.items():
+        ref = float(d["loss." + k])
+        assert abs(v - ref) <= 1e-5 * abs(ref), k
+    for j in range(4):
+        gw, gb = d[f"grad.net.{j}.0.weight"], d[f"grad.net.{j}.0.bias"]
+        assert np.abs(grads[j][0] - gw).max() <= 2e-5 * np.abs(gw).max(), j
+        assert np.abs(grads[j][1] - gb).max() <= 2e-5 * np.abs(gb).max(), j
+
+
+def test_oracle_true_sdf_grads_match_finite_differences():
+    d, params, om = _true_sdf_case()
+    args = (om, d["x"], d["sdf"], d["normals"])
+    _, grads = ot.true_sdf_step_grads(params, *args)
+    rng = np.random.default_rng(9)
+    dirs = [(rng.standard_normal(np.shape(w)), rng.standard_normal(np.shape(b)))
+            for w, b in params]
+    h = 1e-6
+    pp = [(w + h * dw, b + h * db) for (w, b), (dw, db) in zip(params, dirs)]
+    pm = [(w - h * dw, b - h * db) for (w, b), (dw, db) in zip(params, dirs)]
+    fd = (ot.true_sdf_loss_total(pp, *args) - ot.true_sdf_loss_total(pm, *args)) / (2 * h)
+    an = sum((g[0] * dw).sum() + (g[1] * db).sum() for g, (dw, db) in zip(grads, dirs))
+    assert abs(fd - an) <= 1e-5 * abs(an)
