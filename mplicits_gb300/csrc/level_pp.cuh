@@ -302,9 +302,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
                 for (int jj = 0; jj < U; ++jj)
                   v[jj] = GRAD ? __uint_as_float(rr[jj]) : bf16::sin_fast(__uint_as_float(rr[jj]));
                 bf16::store_a_unit<T, U>(sA, m, j0, v);
-                fence_proxy_async_smem();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&achunk[s * kMaxNC + c]);
               } else {
                 const float4* wo4 = reinterpret_cast<const float4*>(wout + j0);
                 float pt = part[s];
@@ -320,18 +317,20 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
                   }
                 }
                 part[s] = pt;
-                if (has_next) {
-                  bf16::layer0_unit<T, GRAD, U>(sA, w0s, WP, m, j0, ch, phase, xn, yn, zn);
-                  fence_proxy_async_smem();
-                  __syncwarp();
-                  if (lane == 0) mbar_arrive(&achunk[s * kMaxNC + c]);
-                }
+                if (has_next) bf16::layer0_unit<T, GRAD, U>(sA, w0s, WP, m, j0, ch, phase, xn, yn, zn);
               }
             }
           }
+          // the slot's next GEMM waits for the whole drain (it overwrites the
+          // accumulator), so the A chunks written here are handed over at once
+          if (l < nh || has_next) fence_proxy_async_smem();
           tc::fence_before_sync();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&dempty[s]);
+          if (lane == 0) {
+            if (l < nh || has_next)
+              for (int c = 0; c < NC; ++c) mbar_arrive(&achunk[s * kMaxNC + c]);
+            mbar_arrive(&dempty[s]);
+          }
           ++ds[s];
           if (l < nh) continue;
 
