@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--skip-train", action="store_true")
     ap.add_argument("--skip-trace", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--only", choices=["train", "trace", "batch"], default=None,
+                    help="run one sub-benchmark alone and print its JSON (profiling runs)")
     ap.add_argument("--profile-only", action="store_true",
                     help="time only the BF16 steps (for profiler runs) and print a short line")
     return ap.parse_args()
@@ -627,6 +629,16 @@ def main():
     __graft_entry__.build()
     N, K, W = args.N, args.steps, max(3, args.warmup)
     levels_np = load_levels_np()
+    if args.only:
+        if args.only == "train":
+            out = train_bench(levels_np, device, K, W, "bf16")
+        elif args.only == "trace":
+            out, _ = trace_bench(levels_np, device, K, W, "bf16")
+        else:
+            out = batch_bench(device, K, W)
+        if rank == 0:
+            print(json.dumps({"only": args.only, **out}), flush=True)
+        return
     from mplicits_gb300 import capi
     if args.bf16_unit:
         capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, args.bf16_unit)
