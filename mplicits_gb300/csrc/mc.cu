@@ -62,38 +62,76 @@ __host__ inline int64_t mc_work_bytes(int64_t N) {
   return align256(R * 4) * 2 + align256(R * 8) * 2 + align256(2 * mc_nblk(N) * 8) + 256;
 }
 
-__device__ __forceinline__ int point_mask(const float* __restrict__ S, int64_t N, int64_t i,
-                                          int64_t j, int64_t k, float iso) {
-  const int64_t p = (i * N + j) * N + k;
-  const bool s = S[p] < iso;
-  int m = 0;
-  if (i + 1 < N && ((S[p + N * N] < iso) != s)) m |= 1;
-  if (j + 1 < N && ((S[p + N] < iso) != s)) m |= 2;
-  if (k + 1 < N && ((S[p + 1] < iso) != s)) m |= 4;
-  return m;
-}
-
-__device__ __forceinline__ int cell_case(const float* __restrict__ S, int64_t N, int64_t i,
-                                         int64_t j, int64_t k, float iso) {
-  int c = 0;
+// Four consecutive values of a row line starting at k (a multiple of 4):
+// one 16-byte load when the grid size is a multiple of 4 (every line then
+// starts 16-byte aligned), otherwise scalar loads; entries past N are 0.
+__device__ __forceinline__ void load4(const float* __restrict__ line, int64_t k, int64_t N,
+                                      bool vec, float (&v)[4]) {
+  if (vec && k + 3 < N) {
+    const float4 f = *reinterpret_cast<const float4*>(line + k);
+    v[0] = f.x;
+    v[1] = f.y;
+    v[2] = f.z;
+    v[3] = f.w;
+  } else {
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int64_t p = ((i + (q & 1)) * N + (j + ((q >> 1) & 1))) * N + (k + ((q >> 2) & 1));
-    c |= (S[p] < iso ? 1 : 0) << q;
+    for (int e = 0; e < 4; ++e) v[e] = k + e < N ? line[k + e] : 0.f;
   }
-  return c;
 }
 
+// Sign bits (S < iso) of the four values of a lane (bits 0..3) and of the
+// value that follows them (bit 4, a separate load that hits the same or the
+// next cache line).
+__device__ __forceinline__ uint32_t sign5(const float* __restrict__ line, int64_t k, int64_t N,
+                                          bool vec, float iso) {
+  float v[4];
+  load4(line, k, N, vec, v);
+  const float nx = k + 4 < N ? line[k + 4] : 0.f;
+  uint32_t b = 0;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) b |= (v[e] < iso ? 1u : 0u) << e;
+  return b | ((k + 4 < N && nx < iso) ? 16u : 0u);
+}
+
+// One warp per row (i, j), 128 points per step (4 per lane): crossing edges
+// owned by each point (along i, j, k, in that order of the mask bits) and the
+// triangle count of each cell (i, j, k) -> (i+1, j+1, k+1).
 __global__ void mc_count_kernel(const float* __restrict__ S, int64_t N, float iso, McWork w) {
   const int lane = threadIdx.x & 31;
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   if (r >= N * N) return;
   const int64_t i = r / N, j = r % N;
-  const bool cells = (i + 1 < N) && (j + 1 < N);
+  const bool has_i = i + 1 < N, has_j = j + 1 < N;
+  const bool vec = (N & 3) == 0;
+  const float* L00 = S + (i * N + j) * N;
+  const float* L10 = L00 + N * N;
+  const float* L01 = L00 + N;
+  const float* L11 = L10 + N;
   int nv = 0, nt = 0;
-  for (int64_t k = lane; k < N; k += 32) {
-    nv += __popc(point_mask(S, N, i, j, k, iso));
-    if (cells && k + 1 < N) nt += c_tri_count[cell_case(S, N, i, j, k, iso)];
+  for (int64_t k0 = 0; k0 < N; k0 += 128) {
+    const int64_t k = k0 + 4 * lane;
+    const uint32_t a = sign5(L00, k, N, vec, iso);
+    const uint32_t b = has_i ? sign5(L10, k, N, vec, iso) : 0u;
+    const uint32_t c = has_j ? sign5(L01, k, N, vec, iso) : 0u;
+    const uint32_t d = has_i && has_j ? sign5(L11, k, N, vec, iso) : 0u;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if (k + e >= N) break;
+      const uint32_t s0 = (a >> e) & 1u;
+      int m = 0;
+      if (has_i && (((b >> e) & 1u) != s0)) m |= 1;
+      if (has_j && (((c >> e) & 1u) != s0)) m |= 2;
+      if (k + e + 1 < N && (((a >> (e + 1)) & 1u) != s0)) m |= 4;
+      nv += __popc(m);
+      if (has_i && has_j && k + e + 1 < N) {
+        // corner q: (i + (q & 1), j + ((q >> 1) & 1), k + e + (q >> 2))
+        const uint32_t cs = ((a >> e) & 1u) | (((b >> e) & 1u) << 1) | (((c >> e) & 1u) << 2) |
+                            (((d >> e) & 1u) << 3) | (((a >> (e + 1)) & 1u) << 4) |
+                            (((b >> (e + 1)) & 1u) << 5) | (((c >> (e + 1)) & 1u) << 6) |
+                            (((d >> (e + 1)) & 1u) << 7);
+        nt += c_tri_count[cs];
+      }
+    }
   }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
@@ -218,12 +256,23 @@ __device__ __forceinline__ float grad_axis(const float* __restrict__ S, int64_t 
 constexpr int kEmitThreads = 128;
 constexpr int kMaxN = 1024;
 
-// one CTA (4 warps) per row r = (i, j)
+// One CTA (4 warps) per row r = (i, j); rows without vertices or triangles
+// return at once.
+//   1. warp w walks line (i + (w >> 1), j + (w & 1)), 128 points per step:
+//      the crossing-edge mask and sign bit of each point and its in-line
+//      vertex prefix (warp scan), into shared memory;
+//   2. the vertices of line (i, j) (interpolation, central-difference
+//      normals);
+//   3. the triangles of the cells of row (i, j): each thread takes four
+//      consecutive cells, the cases come from the sign bits of the four
+//      lines, one block scan orders them.
 __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(
     const float* __restrict__ S, int64_t N, float iso, float vs, float o0, float o1, float o2,
     McWork w, float* __restrict__ verts, float* __restrict__ normals, float* __restrict__ values,
     int32_t* __restrict__ faces, int64_t max_verts, int64_t max_tris) {
-  __shared__ int32_t pre[4][kMaxN];
+  // in-line vertex prefix (< 3 kMaxN) and, per point, the crossing-edge mask
+  // (bits 0-2: along i, j, k) with the point's sign S < iso in bit 3
+  __shared__ int16_t pre[4][kMaxN];
   __shared__ uint8_t msk[4][kMaxN];
   const int64_t r = blockIdx.x;
   const int64_t i = r / N, j = r % N;
@@ -231,24 +280,46 @@ __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const float org[3] = {o0, o1, o2};
 
-  // rows touched by the cells of row (i, j): 0:(i,j) 1:(i,j+1) 2:(i+1,j) 3:(i+1,j+1)
+  // 1. masks, prefixes and signs of the four lines
   {
     const int64_t ri = i + (wid >> 1), rj = j + (wid & 1);
     if (ri < N && rj < N) {
+      const bool vec = (N & 3) == 0;
+      const bool has_i = ri + 1 < N, has_j = rj + 1 < N;
+      const float* L = S + (ri * N + rj) * N;
       int32_t carry = 0;
-      for (int64_t k0 = 0; k0 < N; k0 += 32) {
-        const int64_t k = k0 + lane;
-        const int m = k < N ? point_mask(S, N, ri, rj, k, iso) : 0;
-        int x = __popc(m);
-        const int own = x;
+      for (int64_t k0 = 0; k0 < N; k0 += 128) {
+        const int64_t k = k0 + 4 * lane;
+        const uint32_t a = sign5(L, k, N, vec, iso);
+        const uint32_t b = has_i ? sign5(L + N * N, k, N, vec, iso) : 0u;
+        const uint32_t c = has_j ? sign5(L + N, k, N, vec, iso) : 0u;
+        int m[4], cnt = 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const uint32_t s0 = (a >> e) & 1u;
+          int me = 0;
+          if (k + e < N) {
+            if (has_i && (((b >> e) & 1u) != s0)) me |= 1;
+            if (has_j && (((c >> e) & 1u) != s0)) me |= 2;
+            if (k + e + 1 < N && (((a >> (e + 1)) & 1u) != s0)) me |= 4;
+          }
+          m[e] = me;
+          cnt += __popc(me);
+        }
+        int x = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const int y = __shfl_up_sync(0xffffffffu, x, o);
           if (lane >= o) x += y;
         }
-        if (k < N) {
-          pre[wid][k] = carry + x - own;
-          msk[wid][k] = (uint8_t)m;
+        int run = carry + x - cnt;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (k + e < N) {
+            pre[wid][k + e] = (int16_t)run;
+            msk[wid][k + e] = (uint8_t)(m[e] | (((a >> e) & 1u) << 3));
+          }
+          run += __popc(m[e]);
         }
         carry += __shfl_sync(0xffffffffu, x, 31);
       }
@@ -256,10 +327,10 @@ __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(
   }
   __syncthreads();
 
-  // vertices of row (i, j)
+  // 2. vertices of line (i, j)
   const int64_t vbase = w.pre_v[r];
   for (int64_t k = threadIdx.x; k < N; k += kEmitThreads) {
-    const int m = msk[0][k];
+    const int m = msk[0][k] & 7;
     if (!m) continue;
     int64_t v = vbase + pre[0][k];
     const int64_t p = (i * N + j) * N + k;
@@ -295,31 +366,44 @@ __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(
     }
   }
 
-  // triangles of the cells of row (i, j)
+  // 3. triangles of the cells of row (i, j), four consecutive cells a thread
   if (i + 1 >= N || j + 1 >= N) return;
   int64_t tcarry = w.pre_t[r];
-  for (int64_t k0 = 0; k0 < N - 1; k0 += kEmitThreads) {
-    const int64_t k = k0 + threadIdx.x;
-    int c = 0, nt = 0;
-    if (k < N - 1) {
-      c = cell_case(S, N, i, j, k, iso);
-      nt = c_tri_count[c];
+  for (int64_t k0 = 0; k0 < N - 1; k0 += 4 * kEmitThreads) {
+    const int64_t kb = k0 + 4 * threadIdx.x;
+    int cs[4], nts[4], ntot = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t k = kb + e;
+      int c = 0;
+      if (k < N - 1) {
+        // corner q: (i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2)); line (di, dj) = di * 2 + dj
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          c |= (int)((msk[((q & 1) << 1) | ((q >> 1) & 1)][k + (q >> 2)] >> 3) & 1) << q;
+      }
+      cs[e] = c;
+      nts[e] = k < N - 1 ? c_tri_count[c] : 0;
+      ntot += nts[e];
     }
     int64_t tot;
-    const int64_t off = block_exclusive_scan(nt, &tot);
-    int64_t t = tcarry + off;
-    for (int q = 0; q < nt; ++q, ++t) {
-      if (t >= max_tris) break;
+    int64_t t = tcarry + block_exclusive_scan(ntot, &tot);
 #pragma unroll
-      for (int s = 0; s < 3; ++s) {
-        const int e = c_tri_edges[c][3 * q + s];
-        const int axis = c_edge[e][0];
-        const int row = c_edge[e][1] * 2 + c_edge[e][2];
-        const int64_t kk = k + c_edge[e][3];
-        const int64_t rr = (i + c_edge[e][1]) * N + (j + c_edge[e][2]);
-        const int64_t vid = w.pre_v[rr] + pre[row][kk] +
-                            __popc((int)msk[row][kk] & ((1 << axis) - 1));
-        faces[3 * t + s] = (int32_t)vid;
+    for (int e = 0; e < 4; ++e) {
+      const int64_t k = kb + e;
+      for (int q = 0; q < nts[e]; ++q, ++t) {
+        if (t >= max_tris) break;
+#pragma unroll
+        for (int sidx = 0; sidx < 3; ++sidx) {
+          const int ed = c_tri_edges[cs[e]][3 * q + sidx];
+          const int axis = c_edge[ed][0];
+          const int row = c_edge[ed][1] * 2 + c_edge[ed][2];
+          const int64_t kk = k + c_edge[ed][3];
+          const int64_t rr = (i + c_edge[ed][1]) * N + (j + c_edge[ed][2]);
+          const int64_t vid = w.pre_v[rr] + pre[row][kk] +
+                              __popc((int)msk[row][kk] & ((1 << axis) - 1));
+          faces[3 * t + sidx] = (int32_t)vid;
+        }
       }
     }
     tcarry += tot;
