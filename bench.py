@@ -83,8 +83,8 @@ def load_levels_np():
 
 
 def rank_info():
-    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
-            int(os.environ.get("LOCAL_RANK", "0")))
+    from mplicits_gb300.replicas import rank_info as _ri
+    return _ri()
 
 
 def peaks():
@@ -216,18 +216,25 @@ class Step:
 
 
 def time_steps(step, K, W, with_l0=True):
+    """W untimed steps, then exactly K steps between CUDA events, bracketed
+    by a barrier over the replicas and a device synchronisation on both
+    sides."""
     import torch
+    from mplicits_gb300.replicas import barrier
     for _ in range(W):
         step()
-    torch.cuda.synchronize()
     l0 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(K)] if with_l0 else None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
     e0.record()
     for k in range(K):
         step(l0[k] if with_l0 else None)
     e1.record()
     torch.cuda.synchronize()
+    barrier()
     total_ms = e0.elapsed_time(e1)
     l0_ms = (float(np.mean([a.elapsed_time(b) for a, b in l0]))
              if with_l0 and not step.rec.refine_margin else None)
@@ -645,16 +652,13 @@ def main():
 
     # ---- BF16 fused (the headline)
     bf16 = Step(make_models(levels_np, "bf16", device), N, device, "bf16")
-    if world > 1:
-        dist.barrier()
+    from mplicits_gb300.replicas import barrier, max_over_ranks, replica_value
+    barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         ms, l0_ms = time_steps(bf16, K, W)
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
-    value = world * N ** 3 / (ms * 1e-3)
+    ms = max_over_ranks(ms, device)
+    value = replica_value(N ** 3, ms * 1e-3, world)
     bands = bf16.rec.band_sizes()
     if args.profile_only:
         if rank == 0:
