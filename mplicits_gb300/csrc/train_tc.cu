@@ -734,32 +734,51 @@ __global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const En
   for (int qq = 0; qq < kEndsQ; ++qq)
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[qq][i] = 0.f;
-  for (int64_t b = (int64_t)blockIdx.y * kEndsWarps + warp; b < e.nblocks;
-       b += (int64_t)gridDim.y * kEndsWarps) {
+  // two 64-row blocks per iteration, four rows per lane: every load of an
+  // iteration is issued before the arithmetic that uses it
+  const int64_t stride = (int64_t)gridDim.y * kEndsWarps;
+  for (int64_t b0 = (int64_t)blockIdx.y * kEndsWarps + warp; b0 < e.nblocks; b0 += 2 * stride) {
+    uint4 sv[4], dv[4], d1[4], d2[4];
+    float sd[4];
+    int64_t rowv[4];
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int64_t row = b * 64 + lane + 32 * half;
+    for (int u = 0; u < 4; ++u) {
+      const int64_t b = b0 + (u >> 1) * stride;
+      const int64_t row = b * 64 + lane + 32 * (u & 1);
+      rowv[u] = (b < e.nblocks && (row >> 2) < e.n) ? row : -1;
+      if (rowv[u] < 0) continue;
       const int64_t p = row >> 2;
-      if (p >= e.n) continue;
       const int ch = (int)(row & 3);
       const int64_t off = wg_offset(row, f8 * 8, WP);
-      const float sd = e.seeds[4 * p + ch];
-      fma8(acc[6], *reinterpret_cast<const uint4*>(e.s_last + off), sd);
-      const uint4 dv = *reinterpret_cast<const uint4*>(e.dz + off);
+      sd[u] = e.seeds[4 * p + ch];
+      sv[u] = *reinterpret_cast<const uint4*>(e.s_last + off);
+      dv[u] = *reinterpret_cast<const uint4*>(e.dz + off);
       if (ch == 0) {
-        dbl += sd;
-        add8(acc[0], dv);
-        fma8(acc[3], dv, e.xyz[3 * p + 0]);
-        fma8(acc[4], dv, e.xyz[3 * p + 1]);
-        fma8(acc[5], dv, e.xyz[3 * p + 2]);
-        add8(acc[1], *reinterpret_cast<const uint4*>(e.dz + e.lstride + off));
-        if (nh > 1) add8(acc[2], *reinterpret_cast<const uint4*>(e.dz + 2 * e.lstride + off));
+        d1[u] = *reinterpret_cast<const uint4*>(e.dz + e.lstride + off);
+        if (nh > 1) d2[u] = *reinterpret_cast<const uint4*>(e.dz + 2 * e.lstride + off);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (rowv[u] < 0) continue;
+      const int64_t row = rowv[u];
+      const int64_t p = row >> 2;
+      const int ch = (int)(row & 3);
+      fma8(acc[6], sv[u], sd[u]);
+      if (ch == 0) {
+        dbl += sd[u];
+        add8(acc[0], dv[u]);
+        fma8(acc[3], dv[u], e.xyz[3 * p + 0]);
+        fma8(acc[4], dv[u], e.xyz[3 * p + 1]);
+        fma8(acc[5], dv[u], e.xyz[3 * p + 2]);
+        add8(acc[1], d1[u]);
+        if (nh > 1) add8(acc[2], d2[u]);
       } else if (ch == 1) {
-        add8(acc[3], dv);
+        add8(acc[3], dv[u]);
       } else if (ch == 2) {
-        add8(acc[4], dv);
+        add8(acc[4], dv[u]);
       } else {
-        add8(acc[5], dv);
+        add8(acc[5], dv[u]);
       }
     }
   }
