@@ -20,12 +20,20 @@ namespace mpl {
 namespace {
 
 constexpr int kTile = 128;  // points per tile
-constexpr int kThreads = 256;
 constexpr int kKC = 32;     // K rows per weight chunk
+
+// Thread layout of a width: TX threads along the features (8 features each,
+// two float4 groups 4*TX apart) x 16 along the rows (8 rows each: 4 + 4, 64
+// apart), 2*WP threads in all.
+template <int WP>
+struct Fp32Threads {
+  static constexpr int TX = WP / 8;
+  static constexpr int kThreads = TX * 16;
+};
 
 template <int WP>
 struct Fp32Smem {
-  static constexpr int FPT = WP / 16;  // features per thread
+  static constexpr int FPT = 8;  // features per thread
   static constexpr size_t act = (size_t)WP * kTile * 4;
   static constexpr size_t wbuf = 2ull * kKC * WP * 4;
   static size_t bytes(int nh) {
@@ -35,9 +43,11 @@ struct Fp32Smem {
 };
 
 template <int WP, bool GRAD>
-__global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs a) {
+__global__ void __launch_bounds__(Fp32Threads<WP>::kThreads, 1) level_fp32_kernel(const LevelArgs a) {
   constexpr int PT = GRAD ? kTile / 4 : kTile;  // points per tile
-  constexpr int FPT = WP / 16;
+  constexpr int TX = Fp32Threads<WP>::TX;
+  constexpr int kThreads = Fp32Threads<WP>::kThreads;
+  constexpr int FPT = 8;
   constexpr int NQ = FPT / 4;  // float4 groups of features per thread
   constexpr int CPL = WP / kKC;  // chunks per hidden layer
   extern __shared__ __align__(128) unsigned char smem[];
@@ -54,8 +64,8 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
   uint64_t* bar = reinterpret_cast<uint64_t*>(fout + kTile);     // [2]
 
   const int tid = threadIdx.x;
-  const int tx = tid & 15;
-  const int ty = tid >> 4;
+  const int tx = tid % TX;
+  const int ty = tid / TX;
   const float4* act4 = reinterpret_cast<const float4*>(act);
 
   const int64_t n = level_point_count(a);
@@ -124,7 +134,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
       const float x = pts[pt * 3 + 0], y = pts[pt * 3 + 1], z = pts[pt * 3 + 2];
 #pragma unroll
       for (int f = 0; f < FPT; ++f) {
-        const int j = tx * 4 + (f & 3) + 64 * (f >> 2);
+        const int j = tx * 4 + (f & 3) + 4 * TX * (f >> 2);
         if (ch == 0) {
           float s = __fmul_rn(x, w0t[j]);
           s = __fmaf_rn(y, w0t[WP + j], s);
@@ -162,7 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
             const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
 #pragma unroll
             for (int q = 0; q < NQ; ++q) {
-              const float4 w = w4[kk * (WP / 4) + tx + 16 * q];
+              const float4 w = w4[kk * (WP / 4) + tx + TX * q];
               const float wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
               for (int i = 0; i < 8; ++i)
@@ -190,7 +200,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
             float* dst = a.pre + (((int64_t)layer * n + qq) * 4 + (i & 3)) * WP;
 #pragma unroll
             for (int f4 = 0; f4 < FPT / 4; ++f4) {
-              const int j = tx * 4 + 64 * f4;
+              const int j = tx * 4 + 4 * TX * f4;
               float4 v;
               const bool val = (i & 3) == 0;
               v.x = val ? __fadd_rn(acc[i][4 * f4 + 0], bias[j + 0]) : acc[i][4 * f4 + 0];
@@ -206,7 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
         float4* actw = reinterpret_cast<float4*>(act);
 #pragma unroll
         for (int f = 0; f < FPT; ++f) {
-          const int j = tx * 4 + (f & 3) + 64 * (f >> 2);
+          const int j = tx * 4 + (f & 3) + 4 * TX * (f >> 2);
           const float bj = bias[j];
           float s[8];
           if (GRAD) {
@@ -234,7 +244,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
         for (int i = 0; i < 8; ++i) part[i] = 0.f;
 #pragma unroll
         for (int f = 0; f < FPT; ++f) {
-          const int j = tx * 4 + (f & 3) + 64 * (f >> 2);
+          const int j = tx * 4 + (f & 3) + 4 * TX * (f >> 2);
           const float bj = bias[j], wj = wout[j];
           if (GRAD) {
 #pragma unroll
@@ -256,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1) level_fp32_kernel(const LevelArgs
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
 #pragma unroll
-          for (int o = 8; o >= 1; o >>= 1) part[i] += __shfl_xor_sync(0xffffffffu, part[i], o);
+          for (int o = TX / 2; o >= 1; o >>= 1) part[i] += __shfl_xor_sync(0xffffffffu, part[i], o);
         }
         if (tx == 0) {
 #pragma unroll
@@ -308,7 +318,7 @@ int launch_fp32_wp(const LevelArgs& a, cudaStream_t s) {
     grid = ntiles < grid ? ntiles : grid;
   }
   if (grid <= 0) return MPL_OK;
-  level_fp32_kernel<WP, GRAD><<<(unsigned)grid, kThreads, smem, s>>>(a);
+  level_fp32_kernel<WP, GRAD><<<(unsigned)grid, Fp32Threads<WP>::kThreads, smem, s>>>(a);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
 }
