@@ -69,3 +69,30 @@ def test_large_grid_matches_oracle(lib):
     S = (np.sqrt(X ** 2 + Y ** 2 + Z ** 2) - 0.6 - 0.03 * np.sin(12 * X) * np.sin(12 * Y)
          ).astype(np.float32)
     _assert_same(S)
+
+
+def test_largest_grid_and_densest_line(lib):
+    """N = 1024 (the largest supported grid) with lines whose every edge
+    along k crosses the surface: the in-line vertex prefixes reach their
+    largest values there."""
+    N = 1024
+    S = np.ones((N, N, N), np.float32)
+    alt = np.where(np.arange(N) % 2 == 0, -1.0, 1.0).astype(np.float32)
+    for i, j in ((0, 0), (511, 700), (1022, 1023), (1023, 5)):
+        S[i, j, :] = alt
+    x = np.linspace(-1, 1, N, dtype=np.float32)
+    # and a sphere, so that many rows of cells emit triangles
+    S[:, :, :] = np.minimum(S, (np.sqrt(x[:, None, None] ** 2 + x[None, :, None] ** 2 +
+                                        x[None, None, :] ** 2) - 0.5).astype(np.float32))
+    for i, j in ((0, 0), (511, 700), (1022, 1023), (1023, 5)):
+        S[i, j, :] = alt
+    v, f, _, _ = _assert_same(S)
+    assert v.shape[0] > 1000 and f.shape[0] > 1000
+
+
+def test_grid_limit_is_reported(lib):
+    import ctypes
+    from mplicits_gb300 import capi
+    nb = ctypes.c_int64(0)
+    assert lib.mpl_mc_workspace_bytes(1025, ctypes.byref(nb)) == capi.MPL_ERR_UNSUPPORTED
+    assert lib.mpl_mc_workspace_bytes(1024, ctypes.byref(nb)) == capi.MPL_OK
