@@ -108,28 +108,6 @@ __device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, 
   return false;
 }
 
-// Bounded wait for a single issuing thread (MMA or TMA role): between polls
-// it sleeps for a short, growing time, so that it takes no issue slots from
-// the epilogue warps sharing its scheduler while it waits.
-__device__ __forceinline__ bool mbar_wait_backoff(uint64_t* bar, uint32_t parity, int* status,
-                                                  volatile int* abort_flag) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = global_timer_ns();
-  uint32_t ns = 32;
-  for (uint32_t i = 1;; ++i) {
-    __nanosleep(ns);
-    if (ns < 256) ns <<= 1;
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 15) == 0) {
-      if (*abort_flag) return false;
-      if (global_timer_ns() - t0 > kWaitLimitNs) break;
-    }
-  }
-  report_device_error(status, MPL_ERR_DEVICE_TIMEOUT);
-  *abort_flag = 1;
-  return false;
-}
-
 // warp-uniform bounded wait (all lanes poll; any failure fails the warp)
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* status,
                                           volatile int* abort_flag) {
