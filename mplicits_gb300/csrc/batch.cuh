@@ -227,13 +227,13 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
     // ================= TMA producer: slot constants and weight K chunks ====
     if (lane == 0) {
       int64_t w = 0, tloc = 0;
-      int slot_entry[2] = {-1, -1};
+      int entry0 = -1, entry1 = -1;  // entry whose constants each slot holds
       // the current entry, cached until a tile leaves its range
       int e = -1;
       int64_t e_end = -1;
       const char* pk = nullptr;
       int WP = 0, nh = 0;
-      int64_t hw[kMaxHidden] = {0, 0};
+      int64_t hw0 = 0, hw1 = 0;  // the entry's hidden weight images (kMaxHidden = 2)
       for (int64_t t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x, ++tloc) {
         if (t >= e_end || e < 0 || t < (int64_t)tiles[e]) {
           e = find_entry(tiles, count, t);
@@ -242,14 +242,15 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
           pk = en->packed;
           WP = en->WP;
           nh = en->nh;
-          for (int l = 0; l < kMaxHidden; ++l) hw[l] = en->hw[l];
+          hw0 = en->hw[0];
+          hw1 = en->hw[1];
         }
         const int slot = (int)(tloc & 1);
         if (tloc >= 2 && !bf16::mbar_wait_abort(&cfree[slot], (uint32_t)(((tloc >> 1) - 1) & 1),
                                                 a.status, abort_flag))
           break;
         uint8_t* sl = sSlot + slot * kSlotBytes;
-        if (slot_entry[slot] != e) {
+        if ((slot ? entry1 : entry0) != e) {
           const Entry* en = a.entries + e;
           SlotInfo* info = reinterpret_cast<SlotInfo*>(sl + C::sInfo);
           info->xyz = en->xyz;
@@ -273,7 +274,10 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
             tma_bulk_g2s(sl + C::sBx + l * kBiasTile, pk + en->hbx[l], WP * 32, &cfull[slot]);
           tma_bulk_g2s(sl + C::sW0, pk + en->w0f, WP * 16, &cfull[slot]);
           tma_bulk_g2s(sl + C::sWout, pk + en->wout, WP * 4, &cfull[slot]);
-          slot_entry[slot] = e;
+          if (slot)
+            entry1 = e;
+          else
+            entry0 = e;
         } else {
           mbar_arrive(&cfull[slot]);
         }
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
         const int NC = WP / kKC;
         bool ok = true;
         for (int l = 0; l < nh && ok; ++l) {
-          const char* src = pk + hw[l];
+          const char* src = pk + (l ? hw1 : hw0);
           for (int c = 0; c < NC; ++c, ++w) {
             const int s = (int)(w % S);
             const int64_t u = w / S;
@@ -312,7 +316,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
       const uint32_t aBase = smem_u32(sA);
       const uint32_t wBase = smem_u32(sW);
       int64_t w = 0, g = 0, tloc = 0;
-      int64_t duse[2] = {0, 0};
       uint32_t aph = 0;  // bit c: phase parity of achunk[c]
       bool ok = true;
       for (int64_t t = blockIdx.x; t < total && ok; t += gridDim.x, ++tloc) {
@@ -329,9 +332,10 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
         const uint32_t idesc = tc::idesc_f16kind_f32(kM, WP, Op::kFormat);
         const uint32_t bx = smem_u32(sl + C::sBx);
         for (int l = 0; l < nh && ok; ++l, ++g) {
+          // GEMM g uses accumulator g & 1, whose earlier uses number g >> 1
           const int b = (int)(g & 1);
-          if (duse[b] > 0 && !bf16::mbar_wait_abort(&dempty[b], (uint32_t)((duse[b] - 1) & 1),
-                                                    a.status, abort_flag)) {
+          if (g >= 2 && !bf16::mbar_wait_abort(&dempty[b], (uint32_t)(((g >> 1) - 1) & 1),
+                                               a.status, abort_flag)) {
             ok = false;
             break;
           }
@@ -361,7 +365,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
           }
           if (!ok) break;
           tc::commit(&dfull[b]);
-          ++duse[b];
         }
       }
       tc::commit(finalb);
@@ -373,7 +376,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
     const int m = 32 * q + lane;
     const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
     int64_t g = 0, tloc = 0;
-    int64_t dcnt[2] = {0, 0};
     bool ok = true;
     // first tile: its constants, its point, its layer 0
     int64_t t = blockIdx.x;
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
       float part = 0.f;
       for (int l = 1; l <= nh; ++l, ++g) {
         const int b = (int)(g & 1);
-        if (!bf16::warp_wait(&dfull[b], (uint32_t)(dcnt[b] & 1), a.status, abort_flag)) {
+        if (!bf16::warp_wait(&dfull[b], (uint32_t)((g >> 1) & 1), a.status, abort_flag)) {
           ok = false;
           break;
         }
@@ -478,7 +480,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
         tc::fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(&dempty[b]);
-        ++dcnt[b];
       }
       if (!ok) break;
       // this tile's scalars, then the slot is no longer read by this warp

@@ -338,13 +338,13 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
       const uint32_t aBase = smem_u32(sA);
       const uint32_t wBase = smem_u32(sW);
       int64_t w = 0, g = 0;
-      int64_t duse[2] = {0, 0};
       bool ok = true;
       for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         for (int l = 1; l <= nh && ok; ++l, ++g) {
+          // GEMM g uses accumulator g & 1, whose earlier uses number g >> 1
           const int b = (int)(g & 1);
-          if (duse[b] > 0 &&
-              !mbar_wait_abort(&dempty[b], (uint32_t)((duse[b] - 1) & 1), a.status, abort_flag)) {
+          if (g >= 2 &&
+              !mbar_wait_abort(&dempty[b], (uint32_t)(((g >> 1) - 1) & 1), a.status, abort_flag)) {
             ok = false;
             break;
           }
@@ -375,7 +375,6 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
           }
           if (!ok) break;
           tc::commit(&dfull[b]);
-          ++duse[b];
         }
       }
       // every MMA issued so far must complete before TMEM is released
@@ -392,7 +391,6 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
     const int vlane = lane & ~3;
     const float phase = ch ? 1.57079632679489662f : 0.f;
     int64_t g = 0, tloc = 0;
-    int64_t dcnt[2] = {0, 0};
     bool ok = true;
     // Software pipeline over tiles: layer 0 of tile t+1 is computed chunk by
     // chunk inside the last drain of tile t (the A operand is free once the
@@ -421,7 +419,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
       float part = 0.f;
       for (int l = 1; l <= nh; ++l, ++g) {
         const int b = (int)(g & 1);
-        if (!warp_wait(&dfull[b], (uint32_t)(dcnt[b] & 1), a.status, abort_flag)) {
+        if (!warp_wait(&dfull[b], (uint32_t)((g >> 1) & 1), a.status, abort_flag)) {
           ok = false;
           break;
         }
@@ -490,7 +488,6 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
         tc::fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(&dempty[b]);
-        ++dcnt[b];
       }
       if (!ok) break;
 

@@ -176,13 +176,14 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
     if (lane == 0) {
       const uint32_t wBase = smem_u32(sW);
       int64_t w = 0;
-      int64_t gs[2] = {0, 0};  // GEMMs issued per slot
       bool ok = true;
       for (int64_t r = 0; r < nrounds && ok; ++r) {
         for (int l = 1; l <= nh && ok; ++l) {
           for (int s = 0; s < 2 && ok; ++s) {
             if (tile_of(r, s) >= ntiles) continue;
-            const int64_t k = gs[s];
+            // GEMMs the slot issued before: a slot has a tile in every round
+            // up to its last, so the count follows from (r, l)
+            const int64_t k = r * nh + (l - 1);
             if (k > 0 && !bf16::mbar_wait_abort(&dempty[s], (uint32_t)((k - 1) & 1), a.status,
                                                 abort_flag)) {
               ok = false;
@@ -217,7 +218,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
             }
             if (!ok) break;
             tc::commit(&dfull[s]);
-            ++gs[s];
           }
         }
       }
@@ -233,9 +233,9 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
     const int vlane = lane & ~3;
     const float phase = ch ? 1.57079632679489662f : 0.f;
     const int prow = GRAD ? (m >> 2) : m;
-    int64_t ds[2] = {0, 0};  // GEMMs drained per slot
-    int64_t us[2] = {0, 0};  // output reductions per slot
-    int64_t p[2] = {-1, -1};
+    // point index of each slot's current row (two scalars rather than an
+    // array indexed by the slot, which would live in local memory)
+    int64_t p0 = -1, p1 = -1;
     bool ok = true;
     // layer 0 of the first tile of each slot
     for (int s = 0; s < 2; ++s) {
@@ -243,7 +243,12 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
       if (t >= ntiles) continue;
       float x = 0.f, y = 0.f, z = 0.f;
       const int64_t qi = t * PT + prow;
-      if (qi < n) load_point(a, qi, p[s], x, y, z);
+      int64_t pq = -1;
+      if (qi < n) load_point(a, qi, pq, x, y, z);
+      if (s)
+        p1 = pq;
+      else
+        p0 = pq;
       uint8_t* sA = smem + C::oA + s * C::kABytes;
 #pragma unroll 1
       for (int c = 0; c < NC; ++c) {
@@ -253,13 +258,14 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
         if (lane == 0) mbar_arrive(&achunk[s * kMaxNC + c]);
       }
     }
-    float part[2] = {0.f, 0.f};
     for (int64_t r = 0; r < nrounds && ok; ++r) {
       for (int l = 1; l <= nh && ok; ++l) {
         for (int s = 0; s < 2 && ok; ++s) {
           const int64_t t = tile_of(r, s);
           if (t >= ntiles) continue;
-          if (!bf16::warp_wait(&dfull[s], (uint32_t)(ds[s] & 1), a.status, abort_flag)) {
+          // drains of the slot before this one (as the MMA's GEMM count)
+          const int64_t dn = r * nh + (l - 1);
+          if (!bf16::warp_wait(&dfull[s], (uint32_t)(dn & 1), a.status, abort_flag)) {
             ok = false;
             break;
           }
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
             const int64_t qn = tn * PT + prow;
             if (qn < n) load_point(a, qn, pn, xn, yn, zn);
           }
-          if (l == nh) part[s] = 0.f;
+          float part = 0.f;  // this lane's share of the output dot (last drain)
           const uint32_t taddr = tl + (uint32_t)(s * WP);
 #pragma unroll 1
           for (int c0 = 0; c0 < NC; c0 += 2) {
@@ -304,7 +310,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
                 bf16::store_a_unit<T, U>(sA, m, j0, v);
               } else {
                 const float4* wo4 = reinterpret_cast<const float4*>(wout + j0);
-                float pt = part[s];
+                float pt = part;
 #pragma unroll
                 for (int j4 = 0; j4 < U / 4; ++j4) {
                   const float4 wv = wo4[j4];
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
                     pt = __fmaf_rn(sv, wa[i], pt);
                   }
                 }
-                part[s] = pt;
+                part = pt;
                 if (has_next) bf16::layer0_unit<T, GRAD, U>(sA, w0s, WP, m, j0, ch, phase, xn, yn, zn);
               }
             }
@@ -331,11 +337,10 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
               for (int c = 0; c < NC; ++c) mbar_arrive(&achunk[s * kMaxNC + c]);
             mbar_arrive(&dempty[s]);
           }
-          ++ds[s];
           if (l < nh) continue;
 
           // output layer: combine the feature splits, store, band
-          const int64_t u = us[s]++;
+          const int64_t u = r;  // output reductions of the slot before this one
           float* rs = red + s * (Q > 1 ? Q - 1 : 1) * kM;
           if (h > 0) {
             if (u >= 1 && !bf16::warp_wait(&redfree[s], (uint32_t)((u - 1) & 1), a.status,
@@ -343,7 +348,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
               ok = false;
               break;
             }
-            rs[(h - 1) * kM + m] = part[s];
+            rs[(h - 1) * kM + m] = part;
             __syncwarp();
             if (lane == 0) mbar_arrive(&redfull[s]);
           } else {
@@ -351,12 +356,12 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
               ok = false;
               break;
             }
-            float sum = part[s];
+            float sum = part;
 #pragma unroll
             for (int hh = 0; hh < Q - 1; ++hh) sum = __fadd_rn(sum, rs[hh * kM + m]);
             __syncwarp();
             if (lane == 0) mbar_arrive(&redfree[s]);
-            const int64_t ps = p[s];
+            const int64_t ps = s ? p1 : p0;
             if (GRAD) {
               if (ch && ps >= 0 && a.G) {
                 float* gp = a.G + 3 * ps + (ch - 1);
@@ -367,7 +372,10 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
               store_and_band(a, ps >= 0, ps, __fadd_rn(sum, bout));
             }
           }
-          p[s] = pn;
+          if (s)
+            p1 = pn;
+          else
+            p0 = pn;
         }
       }
     }
