@@ -174,7 +174,12 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
   } else if (warp == kMmaWarp) {
     // ================= MMA issuer ==========================================
     if (lane == 0) {
-      const uint32_t wBase = smem_u32(sW);
+      // descriptor bases; an operand at byte offset o adds o >> 4 (the start
+      // address field, which stays below 2^14 inside shared memory)
+      const uint64_t aDesc = tc::smem_desc(smem_u32(smem + C::oA), 2048u, 128u);
+      const uint64_t wDesc = tc::smem_desc(smem_u32(sW), 128u, 1024u);
+      const uint64_t xDesc = tc::smem_desc(smem_u32(sAx), 2048u, 128u);
+      const uint64_t bxDesc = tc::smem_desc(smem_u32(sBx), 128u, 256u);
       int64_t w = 0;
       bool ok = true;
       for (int64_t r = 0; r < nrounds && ok; ++r) {
@@ -191,11 +196,9 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
             }
             tc::fence_after_sync();
             const uint32_t d_tmem = tmem + (uint32_t)(s * WP);
-            const uint32_t aBase = smem_u32(smem + C::oA + s * C::kABytes);
-            tc::mma_bf16(d_tmem, tc::smem_desc(smem_u32(sAx), 2048u, 128u),
-                         tc::smem_desc(smem_u32(sBx) + (uint32_t)(l - 1) * C::kBxBytes, 128u,
-                                       256u),
-                         IDESC, false);
+            const uint64_t aS = aDesc + (uint64_t)((s * C::kABytes) >> 4);
+            tc::mma_bf16(d_tmem, xDesc, bxDesc + (uint64_t)(((l - 1) * C::kBxBytes) >> 4), IDESC,
+                         false);
             for (int c = 0; c < NC; ++c, ++w) {
               const int st = (int)(w % S);
               if (!bf16::mbar_wait_abort(&achunk[s * kMaxNC + c], (uint32_t)(k & 1), a.status,
@@ -206,14 +209,12 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) level_pp_kernel(con
                 break;
               }
               tc::fence_after_sync();
+              const uint64_t aC = aS + (uint64_t)((c * 8 * 2048) >> 4);
+              const uint64_t wC = wDesc + (uint64_t)((st * C::kStageBytes) >> 4);
 #pragma unroll
-              for (int ks = 0; ks < kKC / 16; ++ks) {
-                const uint64_t ad = tc::smem_desc(aBase + (uint32_t)(c * 8 + ks * 2) * 2048u,
-                                                  2048u, 128u);
-                const uint64_t bd = tc::smem_desc(wBase + (uint32_t)st * C::kStageBytes +
-                                                      (uint32_t)ks * 256u, 128u, 1024u);
-                tc::mma_bf16(d_tmem, ad, bd, IDESC, true);
-              }
+              for (int ks = 0; ks < kKC / 16; ++ks)
+                tc::mma_bf16(d_tmem, aC + (uint64_t)((ks * 2 * 2048) >> 4),
+                             wC + (uint64_t)((ks * 256) >> 4), IDESC, true);
               tc::commit(&wempty[st]);
             }
             if (!ok) break;
