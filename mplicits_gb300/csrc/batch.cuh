@@ -313,8 +313,11 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
   } else if (warp == kMmaWarp) {
     // ================= MMA issuer ==========================================
     if (lane == 0) {
-      const uint32_t aBase = smem_u32(sA);
-      const uint32_t wBase = smem_u32(sW);
+      // descriptor bases; an operand at byte offset o adds o >> 4 (the start
+      // address field, which stays below 2^14 inside shared memory)
+      const uint64_t aDesc = tc::smem_desc(smem_u32(sA), 2048u, 128u);
+      const uint64_t wDesc = tc::smem_desc(smem_u32(sW), 128u, 1024u);
+      const uint64_t xDesc = tc::smem_desc(smem_u32(sAx), 2048u, 128u);
       int64_t w = 0, g = 0, tloc = 0;
       uint32_t aph = 0;  // bit c: phase parity of achunk[c]
       bool ok = true;
@@ -341,8 +344,8 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
           }
           tc::fence_after_sync();
           const uint32_t d_tmem = tmem + (uint32_t)(b * kWPMax);
-          tc::mma_bf16(d_tmem, tc::smem_desc(smem_u32(sAx), 2048u, 128u),
-                       tc::smem_desc(bx + (uint32_t)l * kBiasTile, 128u, 256u), idesc, false);
+          tc::mma_bf16(d_tmem, xDesc, tc::smem_desc(bx + (uint32_t)l * kBiasTile, 128u, 256u),
+                       idesc, false);
           for (int c = 0; c < NC; ++c, ++w) {
             const int s = (int)(w % S);
             if (!bf16::mbar_wait_abort(&achunk[c], (aph >> c) & 1u, a.status, abort_flag) ||
@@ -353,14 +356,12 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) batch_kernel(const 
             }
             aph ^= 1u << c;
             tc::fence_after_sync();
+            const uint64_t aC = aDesc + (uint64_t)((c * 8 * 2048) >> 4);
+            const uint64_t wC = wDesc + (uint64_t)((s * kStageMax) >> 4);
 #pragma unroll
-            for (int ks = 0; ks < kKC / 16; ++ks) {
-              const uint64_t ad = tc::smem_desc(aBase + (uint32_t)(c * 8 + ks * 2) * 2048u,
-                                                2048u, 128u);
-              const uint64_t bd = tc::smem_desc(wBase + (uint32_t)s * kStageMax +
-                                                    (uint32_t)ks * 256u, 128u, 1024u);
-              tc::mma_bf16(d_tmem, ad, bd, idesc, true);
-            }
+            for (int ks = 0; ks < kKC / 16; ++ks)
+              tc::mma_bf16(d_tmem, aC + (uint64_t)((ks * 2 * 2048) >> 4),
+                           wC + (uint64_t)((ks * 256) >> 4), idesc, true);
             tc::commit(&wempty[s]);
           }
           if (!ok) break;

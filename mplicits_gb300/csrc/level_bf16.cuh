@@ -335,8 +335,11 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
   } else if (warp == kMmaWarp) {
     // ================= MMA issuer ==========================================
     if (lane == 0) {
-      const uint32_t aBase = smem_u32(sA);
-      const uint32_t wBase = smem_u32(sW);
+      // descriptor bases; an operand at byte offset o adds o >> 4 (the start
+      // address field, which stays below 2^14 inside shared memory)
+      const uint64_t aDesc = tc::smem_desc(smem_u32(sA), 2048u, 128u);
+      const uint64_t wDesc = tc::smem_desc(smem_u32(sW), 128u, 1024u);
+      const uint64_t xDesc = tc::smem_desc(smem_u32(sAx), 2048u, 128u);
       int64_t w = 0, g = 0;
       bool ok = true;
       for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
           tc::fence_after_sync();
           const uint32_t d_tmem = tmem + (uint32_t)(b * WP);
           // D = bias (ones tile x bias tile), then D += A * W^T chunk by chunk
-          tc::mma_bf16(d_tmem, tc::smem_desc(smem_u32(sAx), 2048u, 128u),
+          tc::mma_bf16(d_tmem, xDesc,
                        tc::smem_desc(smem_u32(sBx) + (uint32_t)(l - 1) * C::kBxBytes, 128u, 256u),
                        IDESC, false);
           for (int c = 0; c < NC; ++c, ++w) {
@@ -362,15 +365,12 @@ __global__ void __launch_bounds__(Epi<U>::kThreads, 1) level_bf16_kernel(const L
               break;
             }
             tc::fence_after_sync();
+            const uint64_t aC = aDesc + (uint64_t)((c * 8 * 2048) >> 4);
+            const uint64_t wC = wDesc + (uint64_t)((s * C::kStageBytes) >> 4);
 #pragma unroll
-            for (int ks = 0; ks < kKC / 16; ++ks) {
-              const uint64_t ad = tc::smem_desc(aBase + (uint32_t)(c * 8 + ks * 2) * 2048u,
-                                                2048u, 128u);
-              const uint64_t bd = tc::smem_desc(wBase + (uint32_t)s * C::kStageBytes +
-                                                    (uint32_t)ks * 256u,
-                                                128u, 1024u);
-              tc::mma_bf16(d_tmem, ad, bd, IDESC, true);
-            }
+            for (int ks = 0; ks < kKC / 16; ++ks)
+              tc::mma_bf16(d_tmem, aC + (uint64_t)((ks * 2 * 2048) >> 4),
+                           wC + (uint64_t)((ks * 256) >> 4), IDESC, true);
             tc::commit(&wempty[s]);
           }
           if (!ok) break;
