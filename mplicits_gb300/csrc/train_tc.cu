@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const En
   const int64_t stride = (int64_t)gridDim.y * kEndsWarps;
   for (int64_t b0 = (int64_t)blockIdx.y * kEndsWarps + warp; b0 < e.nblocks; b0 += 2 * stride) {
     uint4 sv[4], dv[4], d1[4], d2[4];
-    float sd[4];
+    float sd[4], cx[4], cy[4], cz[4];
     int64_t rowv[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -756,21 +756,22 @@ __global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const En
       if (ch == 0) {
         d1[u] = *reinterpret_cast<const uint4*>(e.dz + e.lstride + off);
         if (nh > 1) d2[u] = *reinterpret_cast<const uint4*>(e.dz + 2 * e.lstride + off);
+        cx[u] = e.xyz[3 * p + 0];
+        cy[u] = e.xyz[3 * p + 1];
+        cz[u] = e.xyz[3 * p + 2];
       }
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (rowv[u] < 0) continue;
-      const int64_t row = rowv[u];
-      const int64_t p = row >> 2;
-      const int ch = (int)(row & 3);
+      const int ch = (int)(rowv[u] & 3);
       fma8(acc[6], sv[u], sd[u]);
       if (ch == 0) {
         dbl += sd[u];
         add8(acc[0], dv[u]);
-        fma8(acc[3], dv[u], e.xyz[3 * p + 0]);
-        fma8(acc[4], dv[u], e.xyz[3 * p + 1]);
-        fma8(acc[5], dv[u], e.xyz[3 * p + 2]);
+        fma8(acc[3], dv[u], cx[u]);
+        fma8(acc[4], dv[u], cy[u]);
+        fma8(acc[5], dv[u], cz[u]);
         add8(acc[1], d1[u]);
         if (nh > 1) add8(acc[2], d2[u]);
       } else if (ch == 1) {
