@@ -222,6 +222,26 @@ int mpl_trace_step(const float* S_dev, const int32_t* active_dev, const int32_t*
                    int32_t* count_out_dev, int32_t* hit_out_dev, int32_t* hit_count_dev,
                    int64_t capacity, void* stream);
 
+/* Every remaining marching step of the rays active[0 .. min(*count, n_max))
+ * in one launch, on the tensor cores (BF16 or FP16 operands, `precision`):
+ * per step the `levels` nets (identical hidden widths) are evaluated at the
+ * rays' positions, level l > 0 added only for rays with |partial sum| <
+ * deltas[l - 1] (the band lists of the level launches), then each ray takes
+ * the step of mpl_trace_step (S written, hits appended to hit_out /
+ * *hit_count); with last_is_final set the last of the `steps` steps ends the
+ * budget (state 3).  Gives every ray the result of `steps` rounds of level
+ * launches + mpl_trace_step; a launch keeps one CTA per 128 rays, so it pays
+ * off once few rays are left.  Replaces the tail of the reference's per-level
+ * phases (state.cu:848-880) over IterateSphereTracing_kernel
+ * (kernels.cu:315-398).  MPL_ERR_UNSUPPORTED for widths other than 128/256
+ * or when the levels' constants exceed shared memory. */
+int mpl_trace_march(const MplNet* nets, const void* const* packed_dev, int32_t levels,
+                    const float* deltas, const int32_t* active_dev, const int32_t* count_dev,
+                    int64_t n_max, float* origins_dev, const float* dirs_dev, int32_t* state_dev,
+                    float* S_dev, float eps, float radius, int32_t steps, int32_t last_is_final,
+                    int32_t* hit_out_dev, int32_t* hit_count_dev, int64_t capacity,
+                    int32_t precision, void* stream);
+
 /* Shades every pixel into RGBA8 (little-endian R in the low byte): hits
  * inside [-1,1]^3 with Phong (mode 1) or |normal| colours (mode 0) from the
  * gradients G [P, 3], everything else white.  Replaces Shade_kernel

@@ -130,6 +130,8 @@ SIGNATURES = {
     "mpl_trace_init": (ctypes.c_int, [ctypes.POINTER(MplCamera), _F, _P, _P, _P, _P, _P, _P]),
     "mpl_trace_step": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _F, _F, _I32, _P, _P, _P, _P,
                                       _I64, _P]),
+    "mpl_trace_march": (ctypes.c_int, [ctypes.POINTER(MplNet), _P, _I32, _P, _P, _P, _I64, _P,
+                                       _P, _P, _P, _F, _F, _I32, _I32, _P, _P, _I64, _I32, _P]),
     "mpl_trace_shade": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P]),
     "mpl_train_scratch_floats": (ctypes.c_int, [ctypes.POINTER(MplNet), _I64,
                                                 ctypes.POINTER(_I64)]),

@@ -8,6 +8,7 @@
 // step only touches rays still marching and the finer levels only rays
 // inside their bands (the reference evaluates every level for every pixel).
 #include "level.cuh"
+#include "trace.cuh"
 
 namespace mpl {
 
@@ -17,19 +18,6 @@ struct Basis {
   float eye[3], s[3], u[3], f[3];
   float tx, ty;  // tan(fov/2) * aspect, tan(fov/2)
 };
-
-__device__ __forceinline__ void warp_append(bool keep, int32_t value, int32_t* out,
-                                            int32_t* count, int64_t capacity) {
-  const unsigned m = __ballot_sync(0xffffffffu, keep);
-  const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (lane == 0 && m) base = atomicAdd(count, __popc(m));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (keep) {
-    const int64_t pos = (int64_t)base + __popc(m & ((1u << lane) - 1u));
-    if (pos < capacity) out[pos] = value;
-  }
-}
 
 // Pixel (i, j): NDC x = 2i/W - 1, y = 1 - 2j/H (row 0 at the top), the
 // eye-space direction (x tan(fov/2) aspect, y tan(fov/2), -1) rotated by the
@@ -100,28 +88,9 @@ __global__ void trace_step_kernel(const float* __restrict__ S, const int32_t* __
     int32_t r = 0;
     if (q < n) {
       r = active[q];
-      const float s = S[r];
-      if (fabsf(s) < eps) {
-        hit = true;
-        state[r] = 1;
-      } else {
-        float o[3];
-        float od = 0.f, oo = 0.f;
-        for (int c = 0; c < 3; ++c) {
-          const float d = dir[3 * r + c];
-          o[c] = __fmaf_rn(d, s, org[3 * r + c]);
-          org[3 * r + c] = o[c];
-          od += o[c] * d;
-          oo += o[c] * o[c];
-        }
-        if (oo > R * R && od > 0.0f) {
-          state[r] = 2;
-        } else if (last) {
-          state[r] = 3;  // step budget exhausted
-        } else {
-          keep = true;
-        }
-      }
+      const int outcome = march_ray(S[r], r, org, dir, state, eps, R, last != 0);
+      hit = outcome > 0;
+      keep = outcome == 0;
     }
     warp_append(keep, r, active_out, count_out, capacity);
     warp_append(hit, r, hit_out, hit_count, capacity);

@@ -15,6 +15,12 @@ device-side counts, no host sync) is captured once into a CUDA graph and
 replayed per frame.  Normals of the hits are the sum of the band-gated level
 gradients (forward-mode kernel), as the reference's sum_residual_normals
 (kernels.cu:65-120) sums its per-level normals.
+
+With ``tail_from=k`` (tensor-core precisions), steps k .. max_steps-1 run in
+one persistent launch (mpl_trace_march) that keeps each tile of 128 rays on
+one CTA for all of them: late steps touch few rays, and there the fixed
+latency of the per-level launches dominates.  Every ray gets the same result
+as from the launch-per-level loop.
 """
 
 from __future__ import annotations
@@ -59,7 +65,7 @@ class SphereTracer:
     """Reusable buffers, and the captured step loop, for one image size."""
 
     def __init__(self, levels, deltas, width, height, max_steps=96, eps=1e-4, radius=1.2,
-                 device="cuda", precision=None, graph=True):
+                 device="cuda", precision=None, graph=True, tail_from=None):
         self.levels = list(levels)
         self.deltas = list(deltas)
         if len(self.deltas) < len(self.levels) - 1:
@@ -72,6 +78,7 @@ class SphereTracer:
         self.device = torch.device(device)
         self.precision = precision
         self.use_graph = graph
+        self.tail_from = None if tail_from is None else int(tail_from)
         P, dev = self.P, self.device
         f32 = dict(dtype=torch.float32, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
@@ -120,10 +127,21 @@ class SphereTracer:
             launches += 1
         return launches
 
+    def _tail_step(self):
+        """First step of the persistent marching launch, or None when every
+        step runs as level launches (no tail requested, or a level in FP32)."""
+        if self.tail_from is None or self.tail_from >= self.max_steps:
+            return None
+        precs = {self._prec(m) for m in self.levels}
+        if len(precs) != 1 or precs.pop() == capi.MPL_FP32 or len(self.levels) > 3:
+            return None
+        return max(self.tail_from, 0)
+
     def _march(self, st):
         lib = capi.load()
         launches = 0
-        for k in range(self.max_steps):
+        tail = self._tail_step()
+        for k in range(self.max_steps if tail is None else tail):
             a, b = k & 1, (k + 1) & 1
             launches += self._levels_on(capi.ptr(self.active[a]), capi.ptr(self.counts[a:]),
                                         False, st)
@@ -133,6 +151,24 @@ class SphereTracer:
                 int(k == self.max_steps - 1), capi.ptr(self.active[b]),
                 capi.ptr(self.counts[b:]), capi.ptr(self.hits), capi.ptr(self.counts[2:]),
                 self.P, st), "mpl_trace_step")
+            launches += 1
+        if tail is not None:
+            L = len(self.levels)
+            nets = (capi.MplNet * L)()
+            packed = (ctypes.c_void_p * L)()
+            for i, model in enumerate(self.levels):
+                net, pk = model.packed()
+                nets[i] = net
+                packed[i] = pk.data_ptr()
+            deltas = (ctypes.c_float * max(L - 1, 1))(*[float(d) for d in self.deltas[:L - 1]])
+            a = tail & 1
+            capi.check(lib.mpl_trace_march(
+                nets, ctypes.cast(packed, ctypes.c_void_p), L, ctypes.cast(deltas, ctypes.c_void_p),
+                capi.ptr(self.active[a]), capi.ptr(self.counts[a:]),
+                self.P, capi.ptr(self.org), capi.ptr(self.dir), capi.ptr(self.state),
+                capi.ptr(self.S), self.eps, self.R, self.max_steps - tail, 1,
+                capi.ptr(self.hits), capi.ptr(self.counts[2:]), self.P,
+                self._prec(self.levels[0]), st), "mpl_trace_march")
             launches += 1
         return launches
 

@@ -77,3 +77,48 @@ def test_gpu_tracer_matches_oracle(lib, graph):
                                            np.linalg.norm(g_ref[both], axis=1))
     assert np.median(cos) > 0.9999
     assert img.shape == (64, 96)
+
+
+def _levels(cfg):
+    from mplicits_gb300.model import SIREN
+    levels = []
+    for seed, scale in ((0, 1.0), (1, 0.05), (2, 0.01)):
+        torch.manual_seed(seed)
+        m = SIREN(3, 1, cfg, w0=30)
+        with torch.no_grad():
+            m.net[-1][0].weight.mul_(scale)
+            m.net[-1][0].bias.mul_(scale)
+        levels.append(m.cuda().eval())
+    return levels
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("cfg", [[128, 128], [256, 256, 256]])
+@pytest.mark.parametrize("tail_from,graph", [(0, False), (6, False), (20, True), (39, False)])
+def test_persistent_tail_equals_level_launches(lib, prec, cfg, tail_from, graph):
+    """Steps from tail_from on in one persistent launch give every ray the
+    result of the launch-per-level loop: states, positions, normals and the
+    image are identical, and the hit lists hold the same rays."""
+    from mplicits_gb300 import capi
+    from mplicits_gb300.trace import SphereTracer
+    levels = _levels(cfg)
+    deltas = [0.05, 0.01]
+    W, H = 160, 96
+    cam = _cam((0.3, 0.4, 2.5), W=W, H=H)
+    ref = SphereTracer(levels, deltas, W, H, max_steps=40, eps=1e-3, precision=prec, graph=False)
+    img0, st0 = ref.render(cam)
+    tr = SphereTracer(levels, deltas, W, H, max_steps=40, eps=1e-3, precision=prec, graph=graph,
+                      tail_from=tail_from)
+    for _ in range(2 if graph else 1):
+        img1, st1 = tr.render(cam)
+    torch.cuda.synchronize()
+    assert capi.device_status() == capi.MPL_OK
+    assert (st0 == 1).sum().item() > 100
+    assert torch.equal(st0, st1)
+    assert torch.equal(ref.org, tr.org)
+    assert torch.equal(ref.G, tr.G)
+    assert torch.equal(img0, img1)
+    n0, n1 = int(ref.counts[2]), int(tr.counts[2])
+    assert n0 == n1
+    assert torch.equal(torch.sort(ref.hits[:n0])[0], torch.sort(tr.hits[:n1])[0])
