@@ -459,9 +459,9 @@ def train_cpu_baseline(levels_np, rows=3072, steps=3):
 
 
 # first step of the persistent marching launch (tensor-core precisions): from
-# here on few rays are left; a sweep over 8..40 on the 1920x1080 orbit frames
-# put the fastest frames at 30..40
-TRACE_TAIL_FROM = 30
+# here on few enough rays are left for one tile per SM; a sweep over 8..40 on
+# the 1920x1080 orbit frames put the fastest frames at 32
+TRACE_TAIL_FROM = 32
 
 
 def trace_bench(levels_np, device, K, W, precision="bf16", tail_from=TRACE_TAIL_FROM):

@@ -17,9 +17,12 @@
 // operand (afull, written by the first layer or by the previous drain) and
 // for the previous accumulator to be drained (dempty); the epilogue waits for
 // dfull.  The weights of every level stream through one ring in the MMA's
-// GEMM order (tile, step, level, layer).  The epilogue warps meet at a named
-// barrier after each level's output and after each marching step; its
-// reduction carries the abort decision, so all of them leave together.
+// GEMM order (tile, step, level, layer).  The first layer of level l + 1 is
+// written inside the last drain of level l (the rays have not moved).  The
+// epilogue warps meet at a named barrier twice per step, once with every
+// level's feature-split partial sums written and once after the marching
+// step; its reduction carries the abort decision, so all of them leave
+// together.
 // Every mbarrier wait is bounded (the abort protocol of level_bf16.cuh).
 #include <string.h>
 
@@ -66,8 +69,8 @@ struct Cfg {
   static constexpr uint32_t oW = kABytes;                                // [S] weight chunks
   static constexpr uint32_t oW0 = oW + kStages * kStageBytes;          // float [levels][4][WP]
   static constexpr uint32_t oWout = oW0 + kMaxLevels * WP * 16;        // float [levels][WP]
-  static constexpr uint32_t oRed = oWout + kMaxLevels * WP * 4;        // float [Q-1][128]
-  static constexpr uint32_t oBar = oRed + (Q > 1 ? Q - 1 : 1) * kM * 4;
+  static constexpr uint32_t oRed = oWout + kMaxLevels * WP * 4;        // float [levels][Q][128]
+  static constexpr uint32_t oBar = oRed + kMaxLevels * Q * kM * 4;
   static constexpr uint32_t kNumBars = 2 * kStages + 4;
   static constexpr uint32_t oMisc = oBar + kNumBars * 8;              // tmem slot, abort, bout[3]
   static constexpr uint32_t oAx = (oMisc + 32 + 1023) & ~1023u;        // ones tile
@@ -271,17 +274,18 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
           y = a.org[3 * r + 1];
           z = a.org[3 * r + 2];
         }
-        for (int lev = 0; lev < L && !fail; ++lev) {
-          // layer 0 of this level (the A operand is free: the last GEMM that
-          // read it has been drained)
-          const float* w0 = w0s + lev * 4 * WP;
+        // layer 0 of level 0 (the A operand is free: the last GEMM that read
+        // it has been drained)
 #pragma unroll 1
-          for (int c = 0; c < NC; ++c)
-            bf16::layer0_unit<T, false, U>(sA, w0, WP, m, c * kKC + h * U, 0, 0.f, x, y, z);
-          fence_proxy_async_smem();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(afull);
+        for (int c = 0; c < NC; ++c)
+          bf16::layer0_unit<T, false, U>(sA, w0s, WP, m, c * kKC + h * U, 0, 0.f, x, y, z);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(afull);
+        for (int lev = 0; lev < L; ++lev) {
           const float* wout = wouts + lev * WP;
+          const bool next = lev + 1 < L;  // layer 0 of the next level in the last drain
+          const float* w0n = w0s + (lev + 1) * 4 * WP;
           float part = 0.f;
           for (int l = 1; l <= nh; ++l, ++k) {
             if (!fail && !bf16::warp_wait(dfull, (uint32_t)(k & 1), a.status, abort_flag))
@@ -315,26 +319,31 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
                         part = __fmaf_rn(bf16::sin_fast(__uint_as_float(r2[u][4 * j4 + i])), wa[i],
                                          part);
                     }
+                    if (next) bf16::layer0_unit<T, false, U>(sA, w0n, WP, m, j0, 0, 0.f, x, y, z);
                   }
                 }
               }
             }
-            if (l < nh) fence_proxy_async_smem();
+            const bool hand_over = l < nh || next;  // this drain wrote the next A operand
+            if (hand_over) fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0) {
-              if (l < nh) mbar_arrive(afull);
+              if (hand_over) mbar_arrive(afull);
               mbar_arrive(dempty);
             }
           }
-          // the level's output: feature splits combined by the h = 0 warps
-          if (h > 0) red[(h - 1) * kM + m] = part;
-          fail = epi_any(fail, kEpiThreads);
-          if (fail) break;
-          if (h == 0) {
-            float sum = part;
+          red[(lev * Q + h) * kM + m] = part;
+        }
+        // every level's partial sums written: the h = 0 warps combine the
+        // feature splits, gate the levels by band and take the marching step
+        fail = epi_any(fail, kEpiThreads);
+        if (fail) break;
+        if (h == 0) {
+          for (int lev = 0; lev < L; ++lev) {
+            float sum = red[(lev * Q) * kM + m];
 #pragma unroll
-            for (int hh = 0; hh < Q - 1; ++hh) sum = __fadd_rn(sum, red[hh * kM + m]);
+            for (int hh = 1; hh < Q; ++hh) sum = __fadd_rn(sum, red[(lev * Q + hh) * kM + m]);
             const float f = __fadd_rn(sum, bouts[lev]);
             if (lev == 0) {
               sacc = f;
@@ -344,10 +353,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
               if (gate) sacc = __fadd_rn(sacc, f);
             }
           }
-        }
-        if (fail) break;
-        // the marching step of the rays still alive
-        if (h == 0) {
           int outcome = 0;
           if (alive) {
             a.S[r] = sacc;
