@@ -88,9 +88,9 @@ __global__ void trace_step_kernel(const float* __restrict__ S, const int32_t* __
     int32_t r = 0;
     if (q < n) {
       r = active[q];
-      const int outcome = march_ray(S[r], r, org, dir, state, eps, R, last != 0);
-      hit = outcome > 0;
-      keep = outcome == 0;
+      const int st = march_ray(S[r], r, org, dir, state, eps, R, last != 0);
+      hit = st == 1;
+      keep = st == 0;
     }
     warp_append(keep, r, active_out, count_out, capacity);
     warp_append(hit, r, hit_out, hit_count, capacity);

@@ -21,38 +21,37 @@ __device__ __forceinline__ void warp_append(bool keep, int32_t value, int32_t* o
   }
 }
 
-// One marching step of ray r with SDF value s (renderer/cuda/kernels.cu:
-// 315-398): |s| < eps is a hit (state 1); otherwise the ray advances by s
-// along its direction, and a ray outside the bounding sphere moving outwards
-// is a miss (state 2); on the last step of the budget a ray still marching
-// stops (state 3).  Returns 1 for a hit, 0 for a ray that keeps marching and
-// -1 for a ray that stopped without a hit.
+// One marching step with SDF value s of a ray at o moving along d
+// (renderer/cuda/kernels.cu:315-398): |s| < eps is a hit (state 1);
+// otherwise the ray advances by s along d, and a ray outside the bounding
+// sphere moving outwards is a miss (state 2); on the last step of the budget
+// a ray still marching stops (state 3).  Returns the new state (0: marching).
+__device__ __forceinline__ int march_step(float s, float (&o)[3], const float (&d)[3], float eps,
+                                          float R, bool last) {
+  if (fabsf(s) < eps) return 1;
+  float od = 0.f, oo = 0.f;
+  for (int c = 0; c < 3; ++c) {
+    o[c] = __fmaf_rn(d[c], s, o[c]);
+    od = __fmaf_rn(o[c], d[c], od);
+    oo = __fmaf_rn(o[c], o[c], oo);
+  }
+  if (oo > R * R && od > 0.0f) return 2;
+  return last ? 3 : 0;  // 3: step budget exhausted
+}
+
+// march_step on ray r of the frame's arrays (position, direction, state);
+// returns its new state.
 __device__ __forceinline__ int march_ray(float s, int64_t r, float* __restrict__ org,
                                          const float* __restrict__ dir,
                                          int32_t* __restrict__ state, float eps, float R,
                                          bool last) {
-  if (fabsf(s) < eps) {
-    state[r] = 1;
-    return 1;
-  }
-  float o[3];
-  float od = 0.f, oo = 0.f;
-  for (int c = 0; c < 3; ++c) {
-    const float d = dir[3 * r + c];
-    o[c] = __fmaf_rn(d, s, org[3 * r + c]);
-    org[3 * r + c] = o[c];
-    od = __fmaf_rn(o[c], d, od);
-    oo = __fmaf_rn(o[c], o[c], oo);
-  }
-  if (oo > R * R && od > 0.0f) {
-    state[r] = 2;
-    return -1;
-  }
-  if (last) {
-    state[r] = 3;  // step budget exhausted
-    return -1;
-  }
-  return 0;
+  float o[3] = {org[3 * r + 0], org[3 * r + 1], org[3 * r + 2]};
+  const float d[3] = {dir[3 * r + 0], dir[3 * r + 1], dir[3 * r + 2]};
+  const int st = march_step(s, o, d, eps, R, last);
+  if (st != 1)
+    for (int c = 0; c < 3; ++c) org[3 * r + c] = o[c];
+  if (st != 0) state[r] = st;
+  return st;
 }
 
 }  // namespace mpl

@@ -70,7 +70,8 @@ struct Cfg {
   static constexpr uint32_t oW0 = oW + kStages * kStageBytes;          // float [levels][4][WP]
   static constexpr uint32_t oWout = oW0 + kMaxLevels * WP * 16;        // float [levels][WP]
   static constexpr uint32_t oRed = oWout + kMaxLevels * WP * 4;        // float [levels][Q][128]
-  static constexpr uint32_t oBar = oRed + kMaxLevels * Q * kM * 4;
+  static constexpr uint32_t oPos = oRed + kMaxLevels * Q * kM * 4;    // float4 [128] x, y, z, alive
+  static constexpr uint32_t oBar = oPos + kM * 16;
   static constexpr uint32_t kNumBars = 2 * kStages + 4;
   static constexpr uint32_t oMisc = oBar + kNumBars * 8;              // tmem slot, abort, bout[3]
   static constexpr uint32_t oAx = (oMisc + 32 + 1023) & ~1023u;        // ones tile
@@ -115,6 +116,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
   float* w0s = reinterpret_cast<float*>(smem + C::oW0);
   float* wouts = reinterpret_cast<float*>(smem + C::oWout);
   float* red = reinterpret_cast<float*>(smem + C::oRed);
+  float4* spos = reinterpret_cast<float4*>(smem + C::oPos);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::oBar);
   uint64_t* wfull = bars;           // [S]  TMA -> MMA
   uint64_t* wempty = bars + S;      // [S]  MMA -> TMA
@@ -261,19 +263,28 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
     for (int64_t t = blockIdx.x; t < ntiles && !fail; t += G) {
       const int64_t qi = t * kM + m;
       const int64_t r = qi < n ? (int64_t)a.active[qi] : -1;
-      float sacc = 0.f;   // partial sum of the levels (h = 0 warps)
-      bool gate = false;  // the ray takes the current level (h = 0 warps)
+      // the h = 0 warps own the tile's rays: position, direction and state in
+      // registers, the position shared with the other warps through smem;
+      // the frame's arrays are written when a ray stops
+      float o[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};
+      int ray_state = 2;
+      if (h == 0) {
+        if (r >= 0) {
+          ray_state = a.state[r];
+          for (int c = 0; c < 3; ++c) {
+            o[c] = a.org[3 * r + c];
+            d[c] = a.dir[3 * r + c];
+          }
+        }
+        spos[m] = make_float4(o[0], o[1], o[2], ray_state == 0 ? 1.f : 0.f);
+      }
+      fail = epi_any(fail, kEpiThreads);
       for (int st = 0; st < a.steps && !fail; ++st) {
         // this step's position; rays that have stopped are evaluated where
         // they are and left alone
-        float x = 0.f, y = 0.f, z = 0.f;
-        bool alive = false;
-        if (r >= 0) {
-          alive = a.state[r] == 0;
-          x = a.org[3 * r + 0];
-          y = a.org[3 * r + 1];
-          z = a.org[3 * r + 2];
-        }
+        const float4 pv = spos[m];
+        const float x = pv.x, y = pv.y, z = pv.z;
+        const bool alive = pv.w != 0.f;
         // layer 0 of level 0 (the A operand is free: the last GEMM that read
         // it has been drained)
 #pragma unroll 1
@@ -340,6 +351,8 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
         fail = epi_any(fail, kEpiThreads);
         if (fail) break;
         if (h == 0) {
+          float sacc = 0.f;
+          bool gate = alive;
           for (int lev = 0; lev < L; ++lev) {
             float sum = red[(lev * Q) * kM + m];
 #pragma unroll
@@ -347,19 +360,24 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
             const float f = __fadd_rn(sum, bouts[lev]);
             if (lev == 0) {
               sacc = f;
-              gate = alive;
             } else {
               gate = gate && fabsf(sacc) < a.delta[lev - 1];
               if (gate) sacc = __fadd_rn(sacc, f);
             }
           }
-          int outcome = 0;
+          bool hit = false;
           if (alive) {
-            a.S[r] = sacc;
-            outcome = march_ray(sacc, r, a.org, a.dir, a.state, a.eps, a.R,
-                                a.last_final && st == a.steps - 1);
+            const bool last = st == a.steps - 1;
+            ray_state = march_step(sacc, o, d, a.eps, a.R, a.last_final && last);
+            hit = ray_state == 1;
+            if (ray_state != 0 || last) {
+              a.S[r] = sacc;
+              for (int c = 0; c < 3; ++c) a.org[3 * r + c] = o[c];
+              if (ray_state != 0) a.state[r] = ray_state;
+            }
+            spos[m] = make_float4(o[0], o[1], o[2], ray_state == 0 ? 1.f : 0.f);
           }
-          warp_append(alive && outcome > 0, (int32_t)r, a.hit_out, a.hit_count, a.capacity);
+          warp_append(hit, (int32_t)r, a.hit_out, a.hit_count, a.capacity);
         }
         __threadfence_block();
         fail = epi_any(fail, kEpiThreads);
