@@ -28,6 +28,8 @@
 // MPL_ERR_DEVICE_TIMEOUT and all roles leave their loops.
 #include <string.h>
 
+#include <mutex>
+
 #include "level_bf16.cuh"
 #include "train_loss.cuh"
 
@@ -850,6 +852,33 @@ using namespace mpl::ttc;
 
 static int64_t tc_rows_pad(int64_t n) { return ((n + kPts - 1) / kPts) * kM; }
 
+// A second stream per device (created once) on which the end-layer
+// reductions run next to the weight-gradient GEMM: both read the tiles the
+// fused kernel wrote, the GEMM at most of the DRAM bandwidth and the
+// reductions latency-bound, and both fit on an SM together.  Fork and join
+// are events, so the pair also works inside a captured CUDA graph.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+static int side_stream(SideStream** out) {
+  static SideStream per_device[64];
+  static std::mutex mu;
+  int dev = 0;
+  MPL_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return MPL_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> guard(mu);
+  SideStream& ss = per_device[dev];
+  if (!ss.s) {
+    MPL_CUDA_TRY(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
+    MPL_CUDA_TRY(cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming));
+    MPL_CUDA_TRY(cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming));
+  }
+  *out = &ss;
+  return MPL_OK;
+}
+
 extern "C" int mpl_train_tc_scratch_bytes(const MplNet* net, int64_t n, int64_t* bytes) {
   PackLayout lay;
   int st = make_layout(net, &lay);
@@ -915,6 +944,11 @@ extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const fl
   }
   w.nblocks = rows_pad / 64;
   w.status = a.status;
+  SideStream* side = nullptr;
+  st = side_stream(&side);
+  if (st != MPL_OK) return st;
+  MPL_CUDA_TRY(cudaEventRecord(side->fork, s));
+  MPL_CUDA_TRY(cudaStreamWaitEvent(side->s, side->fork, 0));
   st = WP == 256 ? launch_wgrad<256>(w, nh, s) : launch_wgrad<128>(w, nh, s);
   if (st != MPL_OK) return st;
   // biases, layer 0, output layer
@@ -940,7 +974,10 @@ extern "C" int mpl_train_tc_step(const MplNet* net, const void* packed, const fl
   const int64_t wmax = (e.nblocks + kEndsWarps - 1) / kEndsWarps;
   if (splits > wmax) splits = wmax;
   if (splits < 1) splits = 1;
-  train_tc_ends_kernel<<<dim3((unsigned)(WP / 8), (unsigned)splits), kEndsWarps * 32, 0, s>>>(e);
+  train_tc_ends_kernel<<<dim3((unsigned)(WP / 8), (unsigned)splits), kEndsWarps * 32, 0,
+                         side->s>>>(e);
   MPL_LAUNCH_CHECK();
+  MPL_CUDA_TRY(cudaEventRecord(side->join, side->s));
+  MPL_CUDA_TRY(cudaStreamWaitEvent(s, side->join, 0));
   return MPL_OK;
 }
