@@ -435,7 +435,7 @@ extern "C" int mpl_trace_march(const MplNet* nets, const void* const* packed, in
       return MPL_ERR_UNSUPPORTED;
     a.packed[lev] = (const char*)packed[lev];
   }
-  if (a.lay[0].nh < 1) return MPL_ERR_UNSUPPORTED;
+  if (a.lay[0].nh < 1 || (a.lay[0].WP != 128 && a.lay[0].WP != 256)) return MPL_ERR_UNSUPPORTED;
   for (int lev = 0; lev + 1 < levels; ++lev) a.delta[lev] = deltas[lev];
   a.levels = levels;
   a.active = active;
