@@ -177,7 +177,8 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 //         (LBO 128 B, SBO 256 B).  Multiplied by an A tile whose first two
 //         K columns are 1, one extra K=16 MMA step adds the bias exactly to
 //         ~16 bits.
-//   hwh_l, hbxh_l  hw_l and hbx_l with FP16 elements (the FP16 operand mode).
+//   hwh_l, hbxh_l, hwTh_l  hw_l, hbx_l and hwT_l with FP16 elements (the
+//         FP16 operand mode).
 //   whn_l [WP][WP] FP32 W_l untransposed (j, k): the B operand of the
 //         backward GEMM d_in = d_a W_l.
 struct PackLayout {
@@ -190,6 +191,7 @@ struct PackLayout {
   int64_t hb[MPL_MAX_LAYERS];
   int64_t hw[MPL_MAX_LAYERS], hwT[MPL_MAX_LAYERS], hbx[MPL_MAX_LAYERS];
   int64_t hwh[MPL_MAX_LAYERS], hbxh[MPL_MAX_LAYERS];  // the same two tiles in FP16
+  int64_t hwTh[MPL_MAX_LAYERS];                       // hwT in FP16
   int64_t whn[MPL_MAX_LAYERS];  // FP32 W_l as stored by nn.Linear, [j][k] (backward GEMM)
   int64_t total;
 };

@@ -1,7 +1,9 @@
-// Dispatch of the tensor-core level kernels (templates in level_bf16.cuh and
-// level_pp.cuh): operand type by precision (BF16 or FP16), epilogue unit
-// width by MPL_OPT_BF16_EPILOGUE_UNIT, one or two tiles in flight per CTA by
-// MPL_OPT_TC_TILES_IN_FLIGHT.
+// Dispatch of the tensor-core level kernels (templates in level_bf16.cuh,
+// level_pp.cuh and level_rgrad.cuh): operand type by precision (BF16 or
+// FP16), epilogue unit width by MPL_OPT_BF16_EPILOGUE_UNIT, one or two tiles
+// in flight per CTA by MPL_OPT_TC_TILES_IN_FLIGHT, and for the input gradient
+// the reverse-mode kernel (MPL_OPT_TC_GRAD_REVERSE, levels with one or two
+// hidden GEMMs) or the forward-mode tangent rows of the level kernels.
 #include "level.cuh"
 
 namespace mpl {
@@ -14,9 +16,14 @@ int launch_level_pp_u16_bf16(const LevelArgs& a, cudaStream_t s);
 int launch_level_pp_u32_bf16(const LevelArgs& a, cudaStream_t s);
 int launch_level_pp_u16_f16(const LevelArgs& a, cudaStream_t s);
 int launch_level_pp_u32_f16(const LevelArgs& a, cudaStream_t s);
+int launch_level_rgrad(const LevelArgs& a, bool f16, cudaStream_t s);
 
 int launch_level_tc(const LevelArgs& a, bool f16, cudaStream_t s) {
   if (a.lay.nh == 0) return launch_level_fp32(a, s);  // no hidden GEMM for the tensor cores
+  if (a.grad && option_value(MPL_OPT_TC_GRAD_REVERSE) == 1) {
+    const int st = launch_level_rgrad(a, f16, s);
+    if (st != MPL_ERR_UNSUPPORTED) return st;
+  }
   const bool u32 = option_value(MPL_OPT_BF16_EPILOGUE_UNIT) == 32;
   if (option_value(MPL_OPT_TC_TILES_IN_FLIGHT) == 2) {
     // two tiles per CTA where the level's constants fit next to two A tiles

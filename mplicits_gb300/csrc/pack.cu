@@ -32,7 +32,7 @@ int make_layout(const MplNet* net, PackLayout* lay) {
   lay->b0 = take(WP * 4);
   for (int l = 0; l < MPL_MAX_LAYERS; ++l) {
     lay->wht[l] = lay->bh[l] = lay->hb[l] = lay->hw[l] = lay->hwT[l] = lay->hbx[l] = -1;
-    lay->hwh[l] = lay->hbxh[l] = lay->whn[l] = -1;
+    lay->hwh[l] = lay->hbxh[l] = lay->whn[l] = lay->hwTh[l] = -1;
   }
   for (int l = 1; l <= L - 2; ++l) {
     lay->wht[l] = take((int64_t)WP * WP * 4);
@@ -49,6 +49,7 @@ int make_layout(const MplNet* net, PackLayout* lay) {
     lay->hwh[l] = take((int64_t)WP * WP * 2);
     lay->hbxh[l] = take((int64_t)WP * 16 * 2);
     lay->whn[l] = take((int64_t)WP * WP * 4);
+    lay->hwTh[l] = take((int64_t)WP * WP * 2);
   }
   lay->total = o;
   return MPL_OK;
@@ -77,7 +78,8 @@ __global__ void pack_layer0(const float* __restrict__ W, const float* __restrict
 
 __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict__ b, int out,
                             int in, int WP, float omega, float* wt, float* bh, float* hb,
-                            __nv_bfloat16* hw, __nv_bfloat16* hwT, __half* hwh, float* whn) {
+                            __nv_bfloat16* hw, __nv_bfloat16* hwT, __half* hwh, float* whn,
+                            __half* hwTh) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)WP * WP) return;
   const int n = (int)(e / WP), k = (int)(e % WP);  // n: output row, k: input col
@@ -87,6 +89,7 @@ __global__ void pack_hidden(const float* __restrict__ W, const float* __restrict
   hw[umma_tile_offset(n, k, WP)] = __float2bfloat16_rn(omega * w);
   hwT[umma_tile_offset(k, n, WP)] = __float2bfloat16_rn(omega * w);
   hwh[umma_tile_offset(n, k, WP)] = __float2half_rn(omega * w);
+  hwTh[umma_tile_offset(k, n, WP)] = __float2half_rn(omega * w);
   if (k == 0) {
     const float bb = n < out ? b[n] : 0.f;
     bh[n] = bb;
@@ -159,7 +162,8 @@ extern "C" int mpl_net_pack(const MplNet* net, const float* const* weights,
         weights[l], biases[l], net->dims[l + 1], net->dims[l], WP, net->omega[l],
         (float*)(base + lay.wht[l]), (float*)(base + lay.bh[l]), (float*)(base + lay.hb[l]),
         (__nv_bfloat16*)(base + lay.hw[l]), (__nv_bfloat16*)(base + lay.hwT[l]),
-        (__half*)(base + lay.hwh[l]), (float*)(base + lay.whn[l]));
+        (__half*)(base + lay.hwh[l]), (float*)(base + lay.whn[l]),
+        (__half*)(base + lay.hwTh[l]));
     MPL_LAUNCH_CHECK();
     pack_bias_tile<<<(WP + 127) / 128, 128, 0, s>>>(biases[l], net->dims[l + 1], WP,
                                                     net->omega[l],

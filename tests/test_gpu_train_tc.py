@@ -67,9 +67,12 @@ def test_tensor_core_step_matches_fp32_and_oracle(lib, widths, n):
     ref_l, ref_g = ot.residual_step_grads(params, [30.0] * (len(widths)),
                                           [(fparams, [30.0] * 3)], xs, sdf, nrm)
     keys = ["sdf_constraint", "normal_constraint", "grad_constraint"]
+    # BF16 roundings: a few 1e-3 relative on each gradient; a loss over a
+    # handful of points (squared) sees the tail of that spread
+    ltol = 3e-2 if n >= 100 else 6e-2
     for i, k in enumerate(keys):
         assert abs(res["fp32"][0][i] - ref_l[k]) <= 1e-4 * abs(ref_l[k]) + 1e-6, k
-        assert abs(res["bf16"][0][i] - ref_l[k]) <= 3e-2 * abs(ref_l[k]) + 1e-4, k
+        assert abs(res["bf16"][0][i] - ref_l[k]) <= ltol * abs(ref_l[k]) + 1e-4, k
     for j in range(len(params)):
         for t in range(2):
             ref = ref_g[j][t].reshape(res["bf16"][1][2 * j + t].shape)
