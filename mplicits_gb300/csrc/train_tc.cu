@@ -725,7 +725,7 @@ __device__ __forceinline__ void fma8(float (&acc)[8], const uint4& v, float s) {
 constexpr int kEndsWarps = 8;
 constexpr int kEndsQ = 3 + 3 + 1;  // db_0..db_2, dW0 x/y/z, dWL
 
-__global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const EndsArgs e) {
+__global__ void __launch_bounds__(kEndsWarps * 32, 2) train_tc_ends_kernel(const EndsArgs e) {
   __shared__ float part[kEndsWarps][kEndsQ * 8 + 1];
   const int WP = e.WP, nh = e.nh;
   const int f8 = blockIdx.x;
@@ -736,15 +736,16 @@ __global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const En
   for (int qq = 0; qq < kEndsQ; ++qq)
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[qq][i] = 0.f;
-  // two 64-row blocks per iteration, four rows per lane: every load of an
-  // iteration is issued before the arithmetic that uses it
+  // one 64-row block per iteration, two rows per lane: every load of an
+  // iteration is issued before the arithmetic that uses it, and two CTAs
+  // fit on an SM (128 registers a thread)
   const int64_t stride = (int64_t)gridDim.y * kEndsWarps;
-  for (int64_t b0 = (int64_t)blockIdx.y * kEndsWarps + warp; b0 < e.nblocks; b0 += 2 * stride) {
-    uint4 sv[4], dv[4], d1[4], d2[4];
-    float sd[4], cx[4], cy[4], cz[4];
-    int64_t rowv[4];
+  for (int64_t b0 = (int64_t)blockIdx.y * kEndsWarps + warp; b0 < e.nblocks; b0 += stride) {
+    uint4 sv[2], dv[2], d1[2], d2[2];
+    float sd[2], cx[2], cy[2], cz[2];
+    int64_t rowv[2];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
       const int64_t b = b0 + (u >> 1) * stride;
       const int64_t row = b * 64 + lane + 32 * (u & 1);
       rowv[u] = (b < e.nblocks && (row >> 2) < e.n) ? row : -1;
@@ -764,7 +765,7 @@ __global__ void __launch_bounds__(kEndsWarps * 32) train_tc_ends_kernel(const En
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
       if (rowv[u] < 0) continue;
       const int ch = (int)(rowv[u] & 3);
       fma8(acc[6], sv[u], sd[u]);
