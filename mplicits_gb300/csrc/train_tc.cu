@@ -242,16 +242,21 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
   } else if (warp == kMmaWarp) {
     // ================= MMA issuer ==========================================
     if (lane == 0) {
-      const uint32_t aBase = smem_u32(sA);
-      const uint32_t wBase = smem_u32(sW);
+      // descriptor bases; an operand at byte offset o adds o >> 4 (the start
+      // address field, which stays below 2^14 inside shared memory)
+      const uint64_t aDesc = tc::smem_desc(smem_u32(sA), 2048u, 128u);
+      const uint64_t wDesc = tc::smem_desc(smem_u32(sW), 128u, 1024u);
+      const uint64_t xDesc = tc::smem_desc(smem_u32(sAx), 2048u, 128u);
+      const uint64_t bxDesc = tc::smem_desc(smem_u32(sBx), 128u, 256u);
       int64_t w = 0, g = 0;
-      int64_t uses[2] = {0, 0};
+      int64_t uses0 = 0, uses1 = 0;  // GEMMs issued into each accumulator
       bool ok = true;
       for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         for (int gi = 0; gi < ngemm && ok; ++gi, ++g) {
           const int acc = gi < nh ? gi : nh - 1;
-          if (uses[acc] > 0 &&
-              !bf16::mbar_wait_abort(&freeacc[acc], (uint32_t)((uses[acc] - 1) & 1), a.status,
+          const int64_t used = acc ? uses1 : uses0;
+          if (used > 0 &&
+              !bf16::mbar_wait_abort(&freeacc[acc], (uint32_t)((used - 1) & 1), a.status,
                                      abort_flag)) {
             ok = false;
             break;
@@ -260,9 +265,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
           const uint32_t d_tmem = tmem + (uint32_t)(acc * WP);
           bool acc_on = false;
           if (gi < nh) {
-            tc::mma_bf16(d_tmem, tc::smem_desc(smem_u32(sAx), 2048u, 128u),
-                         tc::smem_desc(smem_u32(sBx) + (uint32_t)gi * C::kBxBytes, 128u, 256u),
-                         IDESC, false);
+            tc::mma_bf16(d_tmem, xDesc, bxDesc + (uint64_t)((gi * C::kBxBytes) >> 4), IDESC, false);
             acc_on = true;
           }
           for (int c = 0; c < NC; ++c, ++w) {
@@ -274,20 +277,22 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
               break;
             }
             tc::fence_after_sync();
+            const uint64_t aC = aDesc + (uint64_t)((c * 8 * 2048) >> 4);
+            const uint64_t wC = wDesc + (uint64_t)((s * C::kStageBytes) >> 4);
 #pragma unroll
             for (int ks = 0; ks < kKC / 16; ++ks) {
-              const uint64_t ad = tc::smem_desc(aBase + (uint32_t)(c * 8 + ks * 2) * 2048u,
-                                                2048u, 128u);
-              const uint64_t bd = tc::smem_desc(wBase + (uint32_t)s * C::kStageBytes +
-                                                    (uint32_t)ks * 256u, 128u, 1024u);
-              tc::mma_bf16(d_tmem, ad, bd, IDESC, acc_on);
+              tc::mma_bf16(d_tmem, aC + (uint64_t)((ks * 2 * 2048) >> 4),
+                           wC + (uint64_t)((ks * 256) >> 4), IDESC, acc_on);
               acc_on = true;
             }
             tc::commit(&wempty[s]);
           }
           if (!ok) break;
           tc::commit(dfull);
-          ++uses[acc];
+          if (acc)
+            ++uses1;
+          else
+            ++uses0;
         }
       }
       tc::commit(finalb);
