@@ -36,7 +36,8 @@ using bf16::kKC;
 using bf16::kM;
 
 constexpr int kMaxLevels = 3;
-constexpr int kStages = 2;
+constexpr int kStages = 3;
+constexpr int kMaxBiasLayers = 8;  // hidden layers whose biases share one K = 16 tile
 
 struct Args {
   const char* packed[kMaxLevels];
@@ -74,10 +75,15 @@ struct Cfg {
   static constexpr uint32_t oBar = oPos + kM * 16;
   static constexpr uint32_t kNumBars = 2 * kStages + 4;
   static constexpr uint32_t oMisc = oBar + kNumBars * 8;              // tmem slot, abort, bout[3]
-  static constexpr uint32_t oAx = (oMisc + 32 + 1023) & ~1023u;        // ones tile
-  static constexpr uint32_t oBx = oAx + kM * 16 * 2;                   // [levels][nh] bias tiles
+  // the biases of every hidden layer j = level * nh + layer - 1 share one
+  // bias tile (K columns 2j, 2j + 1: the two 16-bit pieces of omega*b); the
+  // bias MMA of layer j multiplies it by ones tile j, which is 1 in those
+  // two columns only
+  static constexpr uint32_t oAx = (oMisc + 32 + 1023) & ~1023u;        // [levels*nh] ones tiles
+  static constexpr uint32_t kOnesBytes = kM * 16 * 2;
   static constexpr uint32_t kBxBytes = WP * 16 * 2;
-  static size_t bytes(int levels, int nh) { return oBx + (size_t)levels * nh * kBxBytes; }
+  __host__ __device__ static uint32_t oBx(int layers) { return oAx + (uint32_t)layers * kOnesBytes; }
+  static size_t bytes(int levels, int nh) { return oBx(levels * nh) + kBxBytes; }
 };
 
 // OR of `fail` over the epilogue warps at named barrier 1 (every epilogue
@@ -128,7 +134,6 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::oMisc + 4);
   float* bouts = reinterpret_cast<float*>(smem + C::oMisc + 8);  // [levels] output biases
   uint8_t* sAx = smem + C::oAx;
-  uint8_t* sBx = smem + C::oBx;
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -140,6 +145,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
   const int64_t ntiles = (n + kM - 1) / kM;
   if ((int64_t)blockIdx.x >= ntiles) return;
   const int64_t G = gridDim.x;
+  uint8_t* sBx = smem + C::oBx(L * nh);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -162,17 +168,27 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
       reinterpret_cast<float4*>(w0s + lev * 4 * WP)[i] = g0[i];
       wouts[lev * WP + i] = reinterpret_cast<const float*>(pk + lay.wout)[i];
     }
-    for (int l = 1; l <= nh; ++l) {
-      const uint4* gb = reinterpret_cast<const uint4*>(pk + (kF16 ? lay.hbxh[l] : lay.hbx[l]));
-      uint4* db = reinterpret_cast<uint4*>(sBx + (lev * nh + l - 1) * C::kBxBytes);
-      for (int i = threadIdx.x; i < (int)(C::kBxBytes / 16); i += kThreads) db[i] = gb[i];
-    }
     if (threadIdx.x == 0) bouts[lev] = reinterpret_cast<const float*>(pk + lay.bout)[0];
   }
-  for (int i = threadIdx.x; i < kM * 16; i += kThreads) {
-    const int m = i >> 4, k = i & 15;
-    const uint32_t off = (uint32_t)(((k >> 3) * 16 + (m >> 3)) * 128 + (m & 7) * 16 + (k & 7) * 2);
-    *reinterpret_cast<T*>(sAx + off) = Op::value(k < 2 ? 1.f : 0.f);
+  // the shared bias tile: element (n, k) of a [WP rows][16 K] tile at
+  // ((n/8)*2 + k/8)*128 + (n%8)*16 + (k%8)*2 bytes; layer j's pieces (its
+  // own tile's K columns 0, 1) go to K columns 2j, 2j + 1
+  for (int i = threadIdx.x; i < WP * 16; i += kThreads) {
+    const int nn = i >> 4, kk = i & 15, j = kk >> 1;
+    T v = Op::value(0.f);
+    if (j < L * nh) {
+      const int lev = j / nh, l = j % nh + 1;
+      const T* src = reinterpret_cast<const T*>(
+          a.packed[lev] + (kF16 ? a.lay[lev].hbxh[l] : a.lay[lev].hbx[l]));
+      v = src[(((nn >> 3) * 2) * 128 + (nn & 7) * 16 + (kk & 1) * 2) / 2];
+    }
+    *reinterpret_cast<T*>(sBx + ((nn >> 3) * 2 + (kk >> 3)) * 128 + (nn & 7) * 16 + (kk & 7) * 2) = v;
+  }
+  for (int i = threadIdx.x; i < L * nh * kM * 16; i += kThreads) {
+    const int j = i / (kM * 16), m = (i >> 4) & (kM - 1), k = i & 15;
+    const uint32_t off = (uint32_t)(j * C::kOnesBytes + ((k >> 3) * 16 + (m >> 3)) * 128 +
+                                    (m & 7) * 16 + (k & 7) * 2);
+    *reinterpret_cast<T*>(sAx + off) = Op::value((k >> 1) == j ? 1.f : 0.f);
   }
   fence_proxy_async_smem();
   tc::fence_before_sync();
@@ -227,9 +243,8 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
                 break;
               }
               tc::fence_after_sync();
-              tc::mma_bf16(tmem, xDesc,
-                           bxDesc + (uint64_t)(((lev * nh + l - 1) * C::kBxBytes) >> 4), IDESC,
-                           false);
+              tc::mma_bf16(tmem, xDesc + (uint64_t)(((lev * nh + l - 1) * C::kOnesBytes) >> 4),
+                           bxDesc, IDESC, false);
               for (int c = 0; c < NC; ++c, ++w) {
                 const int s = (int)(w % S);
                 if (!bf16::mbar_wait_abort(&wfull[s], (uint32_t)((w / S) & 1), a.status,
@@ -435,7 +450,9 @@ extern "C" int mpl_trace_march(const MplNet* nets, const void* const* packed, in
       return MPL_ERR_UNSUPPORTED;
     a.packed[lev] = (const char*)packed[lev];
   }
-  if (a.lay[0].nh < 1 || (a.lay[0].WP != 128 && a.lay[0].WP != 256)) return MPL_ERR_UNSUPPORTED;
+  if (a.lay[0].nh < 1 || (a.lay[0].WP != 128 && a.lay[0].WP != 256) ||
+      levels * a.lay[0].nh > march::kMaxBiasLayers)
+    return MPL_ERR_UNSUPPORTED;
   for (int lev = 0; lev + 1 < levels; ++lev) a.delta[lev] = deltas[lev];
   a.levels = levels;
   a.active = active;
