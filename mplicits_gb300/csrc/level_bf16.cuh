@@ -108,6 +108,22 @@ __device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, 
   return false;
 }
 
+// OR of `fail` over the epilogue warps at named barrier 1 (every epilogue
+// thread calls it the same number of times); orders their memory accesses
+// like a CTA barrier, so all of them leave a loop together.
+__device__ __forceinline__ bool epi_any(bool fail, int nthreads) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)fail), "r"(nthreads)
+      : "memory");
+  return r != 0;
+}
+
 // warp-uniform bounded wait (all lanes poll; any failure fails the warp)
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* status,
                                           volatile int* abort_flag) {

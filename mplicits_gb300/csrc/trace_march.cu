@@ -86,22 +86,6 @@ struct Cfg {
   static size_t bytes(int levels, int nh) { return oBx(levels * nh) + kBxBytes; }
 };
 
-// OR of `fail` over the epilogue warps at named barrier 1 (every epilogue
-// thread calls it the same number of times); orders their memory accesses
-// like a CTA barrier.
-__device__ __forceinline__ bool epi_any(bool fail, int nthreads) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, %2, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)fail), "r"(nthreads)
-      : "memory");
-  return r != 0;
-}
-
 template <int WP, int U, typename T>
 __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(const Args a) {
   using C = Cfg<WP, U>;
@@ -293,7 +277,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
         }
         spos[m] = make_float4(o[0], o[1], o[2], ray_state == 0 ? 1.f : 0.f);
       }
-      fail = epi_any(fail, kEpiThreads);
+      fail = bf16::epi_any(fail, kEpiThreads);
       for (int st = 0; st < a.steps && !fail; ++st) {
         // this step's position; rays that have stopped are evaluated where
         // they are and left alone
@@ -363,7 +347,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
         }
         // every level's partial sums written: the h = 0 warps combine the
         // feature splits, gate the levels by band and take the marching step
-        fail = epi_any(fail, kEpiThreads);
+        fail = bf16::epi_any(fail, kEpiThreads);
         if (fail) break;
         if (h == 0) {
           float sacc = 0.f;
@@ -395,7 +379,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
           warp_append(hit, (int32_t)r, a.hit_out, a.hit_count, a.capacity);
         }
         __threadfence_block();
-        fail = epi_any(fail, kEpiThreads);
+        fail = bf16::epi_any(fail, kEpiThreads);
       }
     }
   }

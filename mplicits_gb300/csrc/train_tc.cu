@@ -92,21 +92,6 @@ __host__ __device__ inline uint32_t tmem_cols_for(int cols) {
   return c;
 }
 
-// OR of `fail` over the epilogue warps (named barrier 1); every epilogue
-// thread calls it the same number of times.
-__device__ __forceinline__ bool epi_any(bool fail, int nthreads) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, %2, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)fail), "r"(nthreads)
-      : "memory");
-  return r != 0;
-}
-
 // U values of row m, features j0.. -> BF16 A operand chunk in smem and the
 // same 16-byte words into a weight-gradient tile in HBM.
 template <int U>
@@ -396,7 +381,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
       }
       // ---- output dot over the feature splits, loss and seeds
       if (h > 0 && !fail) red[(h - 1) * kM + m] = part;
-      if (epi_any(fail, kEpiThreads)) break;
+      if (bf16::epi_any(fail, kEpiThreads)) break;
       if (h == 0) {
         float tot = part;
 #pragma unroll
@@ -429,7 +414,7 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) train_tc_kernel(con
         const float mine = ch == 0 ? s_phi : (ch == 1 ? s_g0 : (ch == 2 ? s_g1 : s_g2));
         seedbuf[m] = valid ? mine : 0.f;
       }
-      if (epi_any(false, kEpiThreads)) break;
+      if (bf16::epi_any(false, kEpiThreads)) break;
       const float seed = seedbuf[m];
 
       // ---- backward: dz_l from ds_l and z_l, then GEMM ds_(l-1) = dz_l (omega W_l)
