@@ -64,7 +64,8 @@ def parse():
     ap.add_argument("--skip-train", action="store_true")
     ap.add_argument("--skip-trace", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
-    ap.add_argument("--only", choices=["train", "trace", "batch"], default=None,
+    ap.add_argument("--skip-deltas", action="store_true")
+    ap.add_argument("--only", choices=["train", "trace", "batch", "deltas"], default=None,
                     help="run one sub-benchmark alone and print its JSON (profiling runs)")
     ap.add_argument("--profile-only", action="store_true",
                     help="time only the BF16 steps (for profiler runs) and print a short line")
@@ -458,6 +459,87 @@ def train_cpu_baseline(levels_np, rows=3072, steps=3):
                                       "the CPU (the reference's step restated)"}
 
 
+DELTAS_MESH = (512, 1024)  # theta x phi rings of the triangulated synthetic surface
+DELTAS_MAX, DELTAS_ITERS = 0.05, 100
+
+
+def deltas_mesh():
+    from mplicits_gb300.synthetic import surface_mesh
+    pos, nrm, faces = surface_mesh(*DELTAS_MESH)
+    return np.concatenate([pos, nrm], 1).astype(np.float32), pos, faces
+
+
+def deltas_bench(device, K, W):
+    """calc_deltas over the vertices of a 1,048,576-triangle mesh of the
+    synthetic surface (max_delta 0.05, 100 iterations, eps 2e-4): device
+    resident, and end to end from pinned host rows to host output rows.  The
+    scene (grid) is built once, as the reference builds its raycasting scene
+    once; its build time is reported beside."""
+    import torch
+    from mplicits_gb300.scene import RaycastingScene, calc_deltas
+    V, pos, faces = deltas_mesh()
+    M = V.shape[0]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pos_d, faces_d = torch.from_numpy(pos).to(device), torch.from_numpy(faces).to(device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    scene = RaycastingScene(pos_d, faces_d, device=device)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    Vd = torch.from_numpy(V).to(device)
+    out, iters = calc_deltas(Vd, scene, DELTAS_MAX, DELTAS_ITERS, return_iterations=True)
+    for _ in range(W - 1):
+        calc_deltas(Vd, scene, DELTAS_MAX, DELTAS_ITERS)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(K):
+        calc_deltas(Vd, scene, DELTAS_MAX, DELTAS_ITERS)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    # end to end: pinned host rows in, host rows out, every step
+    host_in = torch.from_numpy(V).pin_memory()
+    host_out = torch.empty(M, 7, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(K):
+        d_in = host_in.to(device, non_blocking=True)
+        host_out.copy_(calc_deltas(d_in, scene, DELTAS_MAX, DELTAS_ITERS), non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / K
+    info = scene.info()
+    d = out[:, 6]
+    return {"workload": f"calc_deltas of {M} vertices of a {faces.shape[0]}-triangle mesh of the "
+                        f"synthetic surface, max_delta {DELTAS_MAX}, {DELTAS_ITERS} iterations, "
+                        "eps 2e-4, uniform-grid scene",
+            "value": M / (ms * 1e-3), "unit": "vertices/s", "ms_per_call": ms,
+            "iterations_run": iters, "ms_per_iteration": ms / max(1, iters),
+            "steps": K, "warmup": W, "dtype": "f32",
+            "scene_build_ms": build_ms, "scene": info,
+            "delta_percentiles": [float(x) for x in
+                                  torch.quantile(d[:1 << 20], torch.tensor(
+                                      [0.0, 0.1, 0.5, 0.9, 1.0], device=device)).cpu()],
+            "e2e": {"value": M / (e2e_ms * 1e-3), "unit": "vertices/s", "ms_per_call": e2e_ms,
+                    "h2d_bytes_per_step": V.nbytes, "d2h_bytes_per_step": M * 7 * 4},
+            "gpu_launches": K * (DELTAS_ITERS + 2)}
+
+
+def deltas_cpu_baseline(iters, n=4096):
+    """The oracle's grid search (C, all host threads) on a seeded subset of
+    the same vertices run for the GPU run's iteration count."""
+    from oracle import deltas as od
+    V, pos, faces = deltas_mesh()
+    idx = np.random.default_rng(2).choice(V.shape[0], n, replace=False)
+    od.calc_deltas(V[idx[:64]], pos, faces, DELTAS_MAX, DELTAS_ITERS, cell=0.005,
+                   force_iters=1)  # compile and warm
+    t0 = time.perf_counter()
+    od.calc_deltas(V[idx], pos, faces, DELTAS_MAX, DELTAS_ITERS, cell=0.005, force_iters=iters)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "vertices/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{n} of the {V.shape[0]} vertices, {iters} iterations, grid cell 0.005, "
+                      "grid build included (C, OpenMP over vertices)"}
+
+
 # first step of the persistent marching launch (tensor-core precisions): from
 # here on few enough rays are left for one tile per SM; a sweep over 8..40 on
 # the 1920x1080 orbit frames put the fastest frames at 32
@@ -649,6 +731,10 @@ def main():
             out = train_bench(levels_np, device, K, W, "bf16")
         elif args.only == "trace":
             out, _ = trace_bench(levels_np, device, K, W, "bf16")
+        elif args.only == "deltas":
+            out = deltas_bench(device, K, W)
+            if rank == 0 and not args.skip_cpu:
+                out["cpu_baseline"] = deltas_cpu_baseline(out["iterations_run"])
         else:
             out = batch_bench(device, K, W)
         if rank == 0:
@@ -728,6 +814,12 @@ def main():
     if not args.skip_batch:
         batched = batch_bench(device, K, W)
 
+    neigh = None
+    if not args.skip_deltas:
+        neigh = deltas_bench(device, K, W)
+        if rank == 0 and not args.skip_cpu:
+            neigh["cpu_baseline"] = deltas_cpu_baseline(neigh["iterations_run"])
+
     # ---- roofline of the dominant kernel (level 0 over the full grid)
     peak_tf, hbm, src = peaks()
     achieved_tf = FLOP_PER_POINT * N ** 3 / (l0_ms * 1e-3) / 1e12
@@ -780,6 +872,7 @@ def main():
             "training": training,
             "sphere_tracing": tracing,
             "batched_models": batched,
+            "neighbourhood_deltas": neigh,
             "gpu_launches": K * KERNEL_LAUNCHES_PER_STEP,
             "clocks": clk.summary(),
         }

@@ -346,6 +346,44 @@ int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* g
                   float* const* exp_avg_dev, float* const* exp_avg_sq_dev, const int64_t* numel,
                   float lr, float beta1, float beta2, float eps, int64_t step, void* stream);
 
+/* ---- triangle scene and the tubular-neighbourhood deltas ----------------- */
+/* Stand-in for the open3d RaycastingScene the neighbourhood trainers build
+ * (experiment_scripts/train_sdf_on_neighborhood.py:145-146) and query with
+ * compute_distance: a uniform grid over the mesh (cell side `cell`, or twice
+ * the mean edge length when cell == 0) whose cells list the triangles that
+ * overlap them.  Setup, not the hot path: mpl_scene_create synchronises
+ * `stream` and allocates the scene's device memory itself (the one exception
+ * to the caller-owned-memory rule; mpl_scene_destroy frees it).  positions
+ * [n_positions, 3] float32, faces [n_faces, 3] int32; a face index outside
+ * [0, n_positions) gives MPL_ERR_INVALID_ARG.  The scene copies the corners:
+ * the inputs may be freed after the call. */
+typedef struct MplScene MplScene;
+int mpl_scene_create(const float* positions_dev, int64_t n_positions, const int32_t* faces_dev,
+                     int64_t n_faces, float cell, MplScene** scene, void* stream);
+int mpl_scene_destroy(MplScene* scene);
+/* grid geometry (host values; any pointer may be null) */
+int mpl_scene_info(const MplScene* scene, float* lo3, float* cell, int32_t* dims3,
+                   int64_t* n_refs);
+/* Unsigned distance from each point [n, 3] to the nearest triangle
+ * (RaycastingScene.compute_distance), float32, exact for the float32
+ * closest-point computation stated in the source; NaN for a point with a
+ * non-finite coordinate. */
+int mpl_scene_compute_distance(const MplScene* scene, const float* points_dev, int64_t n,
+                               float* distances_dev, void* stream);
+/* calc_deltas (experiment_scripts/utils.py:46-89): out [n_vertices, cols + 1]
+ * is the input rows (cols >= 6: xyz, normal, ...) with the normal
+ * normalised and the bisected neighbourhood radius appended.  step0 =
+ * max_delta / n_iters in float32; the loop runs while max(delta) <
+ * max_delta, n_iters times at most (the reference uses eps 2e-4).  scratch
+ * is sized by mpl_calc_deltas_scratch_bytes (256-byte aligned).
+ * iterations_dev (nullable, device int32) receives the number of
+ * iterations run.  Results equal the reference loop over an exact
+ * nearest-triangle distance bit for bit. */
+int mpl_calc_deltas_scratch_bytes(int64_t n_vertices, int32_t n_iters, int64_t* bytes);
+int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev, int64_t n_vertices,
+                    int32_t cols, float max_delta, int32_t n_iters, float eps, void* scratch_dev,
+                    float* out_dev, int32_t* iterations_dev, void* stream);
+
 /* ---- batched evaluation of many levels of many models ------------------- */
 /* No single reference entry point: this replaces the reference's one launch
  * chain per model and per level (renderer/cuda/gemms.cu:5-192 NeuralImplicit,

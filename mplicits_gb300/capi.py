@@ -148,6 +148,13 @@ SIGNATURES = {
     "mpl_train_batch": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _F, _F, _I32,
                                        ctypes.c_uint64, _P, _P, _P, _P]),
     "mpl_adam_step": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _F, _F, _F, _F, _I64, _P]),
+    "mpl_scene_create": (ctypes.c_int, [_P, _I64, _P, _I64, _F, ctypes.POINTER(_P), _P]),
+    "mpl_scene_destroy": (ctypes.c_int, [_P]),
+    "mpl_scene_info": (ctypes.c_int, [_P, ctypes.POINTER(_F), ctypes.POINTER(_F),
+                                      ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
+    "mpl_scene_compute_distance": (ctypes.c_int, [_P, _P, _I64, _P, _P]),
+    "mpl_calc_deltas_scratch_bytes": (ctypes.c_int, [_I64, _I32, ctypes.POINTER(_I64)]),
+    "mpl_calc_deltas": (ctypes.c_int, [_P, _P, _I64, _I32, _F, _I32, _F, _P, _P, _P, _P]),
     "mpl_batch_workspace_bytes": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
     "mpl_batch_prepare": (ctypes.c_int, [ctypes.POINTER(MplBatchEntry), _I32, _I32, _P, _I64,
                                          ctypes.POINTER(MplBatchPlan), _P]),

@@ -24,6 +24,40 @@ def surface_points(n, rng, noise=0.0):
     normals, and optional Gaussian position noise (normals unchanged)."""
     theta = np.arccos(1.0 - 2.0 * rng.random(n))
     phi = 2.0 * np.pi * rng.random(n)
+    pts, nrm = _point_normal(theta, phi)
+    if noise > 0:
+        pts = pts + rng.normal(0.0, noise, pts.shape)
+    return pts.astype(np.float32), nrm.astype(np.float32)
+
+
+def surface_mesh(n_theta, n_phi):
+    """The surface as a closed triangle mesh: a pole vertex at each end and
+    ``n_theta - 1`` rings of ``n_phi`` vertices, every quad split in two.
+    Returns float32 positions [V, 3], unit normals [V, 3] and int32 faces
+    [F, 3] (V = (n_theta - 1) n_phi + 2, F = 2 (n_theta - 1) n_phi)."""
+    if n_theta < 2 or n_phi < 3:
+        raise ValueError("surface_mesh needs n_theta >= 2 and n_phi >= 3")
+    t = np.pi * np.arange(1, n_theta) / n_theta
+    p = 2.0 * np.pi * np.arange(n_phi) / n_phi
+    theta = np.concatenate([[0.0], np.repeat(t, n_phi), [np.pi]])
+    phi = np.concatenate([[0.0], np.tile(p, n_theta - 1), [0.0]])
+    pts, nrm = _point_normal(theta, phi)
+    rings = n_theta - 1
+    ring = lambda i: 1 + i * n_phi  # noqa: E731  first vertex of ring i
+    j = np.arange(n_phi)
+    jn = (j + 1) % n_phi
+    faces = [np.stack([np.zeros(n_phi, np.int64), ring(0) + j, ring(0) + jn], 1)]
+    for i in range(rings - 1):
+        a, b = ring(i) + j, ring(i) + jn
+        c, d = ring(i + 1) + j, ring(i + 1) + jn
+        faces += [np.stack([a, c, b], 1), np.stack([b, c, d], 1)]
+    south = 1 + rings * n_phi
+    faces.append(np.stack([ring(rings - 1) + j, np.full(n_phi, south), ring(rings - 1) + jn], 1))
+    return (pts.astype(np.float32), nrm.astype(np.float32),
+            np.concatenate(faces).astype(np.int32))
+
+
+def _point_normal(theta, phi):
     r = radius(theta, phi)
     st, ct, sp, cp = np.sin(theta), np.cos(theta), np.sin(phi), np.cos(phi)
     rhat = np.stack([st * cp, st * sp, ct], 1)
@@ -34,10 +68,7 @@ def surface_points(n, rng, noise=0.0):
     st_safe = np.where(np.abs(st) < 1e-9, 1e-9, st)
     g = rhat - (dr_dt / r)[:, None] * that - (dr_dp / (r * st_safe))[:, None] * phat
     nrm = g / np.linalg.norm(g, axis=1, keepdims=True)
-    pts = r[:, None] * rhat
-    if noise > 0:
-        pts = pts + rng.normal(0.0, noise, pts.shape)
-    return pts.astype(np.float32), nrm.astype(np.float32)
+    return r[:, None] * rhat, nrm
 
 
 def inside_sign(p):

@@ -1,0 +1,94 @@
+"""The calc_deltas oracle against the reference's own loop (golden vectors)
+and its point-triangle distance against float64 geometry."""
+
+import os
+
+import numpy as np
+import pytest
+
+from oracle import deltas as od
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "calc_deltas.npz")
+
+
+def _golden():
+    g = np.load(GOLDEN)
+    for name in g["cases"]:
+        yield str(name), {k.split("__", 1)[1]: g[k] for k in g.files if k.startswith(f"{name}__")}
+
+
+@pytest.mark.parametrize("cell", [0.0, 0.03, 0.11])
+def test_oracle_equals_reference_loop(cell):
+    for name, c in _golden():
+        out, it = od.calc_deltas(c["vertices"], c["positions"], c["faces"], c["max_delta"],
+                                 int(c["n_iters"]), cell=cell)
+        assert it == int(c["iterations"]), name
+        np.testing.assert_array_equal(out, c["out"], err_msg=name)
+
+
+def _seg_dist(p, a, b):
+    ab = b - a
+    t = np.clip(np.sum((p - a) * ab, -1) / np.maximum(np.sum(ab * ab, -1), 1e-300), 0.0, 1.0)
+    return np.linalg.norm(p - (a + t[..., None] * ab), axis=-1)
+
+
+def _tri_dist64(p, a, b, c):
+    """float64: distance to the plane where the projection falls inside,
+    else the nearest of the three edges."""
+    n = np.cross(b - a, c - a)
+    n = n / np.linalg.norm(n, axis=-1, keepdims=True)
+    h = np.sum((p - a) * n, -1)
+    q = p - h[..., None] * n
+    inside = True
+    for u, v in ((a, b), (b, c), (c, a)):
+        inside = inside & (np.sum(np.cross(v - u, q - u) * n, -1) >= 0)
+    edge = np.minimum(np.minimum(_seg_dist(p, a, b), _seg_dist(p, b, c)), _seg_dist(p, c, a))
+    return np.where(inside, np.abs(h), edge)
+
+
+def test_triangle_distance_against_float64():
+    rng = np.random.default_rng(3)
+    n = 4000
+    a, b, c = (rng.uniform(-1, 1, (n, 3)) for _ in range(3))
+    p = rng.uniform(-1.5, 1.5, (n, 3))
+    a32, b32, c32, p32 = (x.astype(np.float32) for x in (a, b, c, p))
+    want = _tri_dist64(*(x.astype(np.float64) for x in (p32, a32, b32, c32)))
+    got = np.array([od.tri_dist(p32[i], a32[i], b32[i], c32[i]) for i in range(n)])
+    assert np.max(np.abs(got - want)) < 2e-6
+    # the vertices and points on the triangle are at distance ~0
+    for i in range(50):
+        for v in (a32[i], b32[i], c32[i], (a32[i] + b32[i]) / 2):
+            assert od.tri_dist(v, a32[i], b32[i], c32[i]) < 1e-6
+
+
+def test_compute_distance_mesh_against_float64():
+    from mplicits_gb300 import synthetic
+    pos, _, faces = synthetic.surface_mesh(10, 16)
+    rng = np.random.default_rng(4)
+    pts = rng.uniform(-0.9, 0.9, (300, 3)).astype(np.float32)
+    got = od.compute_distance(pos, faces, pts)
+    P = pos.astype(np.float64)
+    A, B, C = P[faces[:, 0]], P[faces[:, 1]], P[faces[:, 2]]
+    want = np.min(_tri_dist64(pts.astype(np.float64)[:, None], A[None], B[None], C[None]), 1)
+    assert np.max(np.abs(got - want)) < 2e-6
+    bad = od.compute_distance(pos, faces, np.array([[np.nan, 0, 0]], np.float32))
+    assert np.isnan(bad[0])
+
+
+def test_slab_converges_to_half_gap():
+    from golden.make_calc_deltas import slab
+    pos, nrm, faces = slab(6, 0.08)
+    out, _ = od.calc_deltas(np.concatenate([pos, nrm], 1), pos, faces, 0.2, 100, cell=0.05)
+    # the inscribed ball between two sheets has radius gap / 2; the bisection
+    # lands within eps of it
+    assert np.all(np.abs(out[:, 6] - 0.04) < 3e-4)
+
+
+def test_arguments():
+    pos, faces = np.zeros((3, 3), np.float32), np.array([[0, 1, 2]], np.int32)
+    with pytest.raises(ValueError):
+        od.calc_deltas(np.zeros((0, 6), np.float32), pos, faces)
+    with pytest.raises(ValueError):
+        od.calc_deltas(np.zeros((2, 5), np.float32), pos, faces)
+    with pytest.raises(ValueError):
+        od.calc_deltas(np.zeros((2, 6), np.float32), pos, np.array([[0, 1, 3]], np.int32))
