@@ -11,9 +11,11 @@
 // Scene: a uniform grid of cubic cells over the mesh's bounding box (one cell
 // of margin on every side).  Each cell lists the triangles whose bounding box,
 // grown by a relative 1e-5, overlaps it; the lists are stored in cell order as
-// the triangles' corner coordinates (three float4 per entry), so a query reads
-// a cell's triangles as one contiguous run.  Built on the device by a count
-// pass, an exclusive scan and a fill pass.
+// the triangles' corner coordinates (three float4 per entry) beside one
+// bounding sphere per entry (a separate float4 array, read first), so a query
+// reads a cell's triangles as one contiguous run and computes the exact
+// distance only for entries whose sphere comes near enough.  Built on the
+// device by a count pass, an exclusive scan and a fill pass.
 //
 // Distance: the closest point of each triangle by the Voronoi-region method
 // of C. Ericson, "Real-Time Collision Detection" (2005), section 5.1.5, in
@@ -22,13 +24,12 @@
 // visits the cells within a radius R of q in shells of growing Chebyshev
 // distance from q's cell, skipping cells whose box is farther than R.
 //
-// Decision of one bisection step: with R = delta + eps plus a margin, every
-// triangle that can change |delta - D| > eps is visited (a triangle farther
-// than R has float distance above delta + eps, so it is neither the minimum
-// nor able to flip the comparison).  The search stops at the first triangle
-// with delta - d > eps: then D <= d and the comparison holds for the true
-// minimum too.  The result equals the brute-force minimum's comparison bit for
-// bit.
+// Decision of one bisection step (shrink_step): |delta - D| > eps for the
+// minimum D is rewritten as "some triangle nearer than delta - eps, or none
+// within delta + eps" (exact in float32, see shrink_step), so the search
+// stops at the first near triangle and, once one triangle within delta + eps
+// is found, ignores everything beyond delta - eps.  The result equals the
+// brute-force minimum's comparison bit for bit.
 //
 // One launch per iteration: the stopping rule max(delta) < max_delta couples
 // all vertices, so launch i reads the maximum left by launch i - 1 (a float
@@ -51,6 +52,7 @@ struct MplScene {
   int64_t n_refs;
   uint32_t* start;  // [cells + 1] offsets into tris (in entries)
   float4* tris;     // [n_refs * 3] corners a, b, c (w unused)
+  float4* bound;    // [n_refs] bounding sphere: centre, radius
 };
 
 namespace mpl {
@@ -69,6 +71,7 @@ struct View {
   int32_t dim[3];
   const uint32_t* __restrict__ start;
   const float4* __restrict__ tris;
+  const float4* __restrict__ bound;
 };
 
 // ---- the exact float32 point-triangle distance -----------------------------
@@ -142,10 +145,10 @@ __device__ __forceinline__ float cell_box_d2(const View& S, V3 q, int x, int y, 
   return gx * gx + gy * gy + gz * gz;
 }
 
-// Minimum distance from q over the triangles listed in the cells within R of
-// q, visited in shells around q's cell.  With `early`, returns -1 at the first
-// triangle with delta - d > eps.
-__device__ float bounded_min(const View& S, V3 q, float R, bool early, float delta, float eps) {
+// Visits the cells within R of q in shells of growing Chebyshev distance from
+// q's cell (clamped to the grid); visit(cell, box_d2) returns true to stop.
+template <class Visit>
+__device__ __forceinline__ void walk_cells(const View& S, V3 q, float R, Visit&& visit) {
   int lo[3], hi[3], c[3];
   const float qa[3] = {q.x, q.y, q.z};
 #pragma unroll
@@ -157,8 +160,6 @@ __device__ float bounded_min(const View& S, V3 q, float R, bool early, float del
   int rmax = 0;
 #pragma unroll
   for (int k = 0; k < 3; ++k) rmax = max(rmax, max(c[k] - lo[k], hi[k] - c[k]));
-  const float R2 = R * R;
-  float best = INFINITY;
   for (int r = 0; r <= rmax; ++r) {
     const int z0 = max(lo[2], c[2] - r), z1 = min(hi[2], c[2] + r);
     const int y0 = max(lo[1], c[1] - r), y1 = min(hi[1], c[1] + r);
@@ -172,28 +173,86 @@ __device__ float bounded_min(const View& S, V3 q, float R, bool early, float del
         const int xstep = full ? 1 : max(2 * r, 1);
         for (int x = xs; x <= xe; x += xstep) {
           if (x < lo[0] || x > hi[0]) continue;
-          if (cell_box_d2(S, q, x, y, z) > R2) continue;
           const int64_t cell = ((int64_t)z * S.dim[1] + y) * S.dim[0] + x;
-          const uint32_t e0 = S.start[cell], e1 = S.start[cell + 1];
-          for (uint32_t e = e0; e < e1; ++e) {
-            const float4 A = S.tris[3 * (int64_t)e], B = S.tris[3 * (int64_t)e + 1],
-                         C = S.tris[3 * (int64_t)e + 2];
-            const float d = __fsqrt_rn(tri_dist2(q, {A.x, A.y, A.z}, {B.x, B.y, B.z},
-                                                 {C.x, C.y, C.z}));
-            if (d < best) best = d;
-            if (early && __fsub_rn(delta, d) > eps) return -1.f;
-          }
+          if (visit(cell, cell_box_d2(S, q, x, y, z))) return;
         }
       }
     }
   }
+}
+
+__device__ __forceinline__ float entry_dist(const View& S, V3 q, uint32_t e) {
+  const float4 A = S.tris[3 * (int64_t)e], B = S.tris[3 * (int64_t)e + 1],
+               C = S.tris[3 * (int64_t)e + 2];
+  return __fsqrt_rn(tri_dist2(q, {A.x, A.y, A.z}, {B.x, B.y, B.z}, {C.x, C.y, C.z}));
+}
+
+// squared distance from q to an entry's bounding-sphere centre
+__device__ __forceinline__ float centre_d2(V3 q, float4 b) {
+  const float dx = q.x - b.x, dy = q.y - b.y, dz = q.z - b.z;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// margin added to a search radius: far above the rounding of the cell, box
+// and sphere arithmetic at the coordinates' magnitude
+__device__ __forceinline__ float margin(V3 q, float h) {
+  return 1e-5f * (fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z))) + h);
+}
+
+// Minimum distance from q over the triangles within R of q (INFINITY when
+// none).  An entry whose bounding sphere lies farther than the best so far
+// cannot lower it and is skipped; the minimum is the same.
+__device__ float nearest(const View& S, V3 q, float R) {
+  const float m = margin(q, S.h);
+  float best = INFINITY;
+  walk_cells(S, q, R, [&](int64_t cell, float box_d2) {
+    const float lim = fminf(best * 1.0001f + m, R);
+    if (box_d2 > lim * lim) return false;
+    const uint32_t e0 = S.start[cell], e1 = S.start[cell + 1];
+    for (uint32_t e = e0; e < e1; ++e) {
+      const float4 b = S.bound[e];
+      const float l = (fminf(best * 1.0001f + m, R) + b.w) * 1.00002f;
+      if (centre_d2(q, b) > l * l) continue;
+      const float d = entry_dist(S, q, e);
+      if (d < best) best = d;
+    }
+    return false;
+  });
   return best;
 }
 
-// margin added to a search radius: far above the rounding of the cell and
-// box arithmetic at the coordinates' magnitude
-__device__ __forceinline__ float search_radius(float r, V3 q, float h) {
-  return r * 1.0001f + 1e-5f * (fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z))) + h);
+// One bisection decision, |delta - D| > eps for D the minimum distance over
+// all triangles, in float32.  With d_t each triangle's distance and the
+// rounded differences monotone in d_t, it equals
+//   (some t has delta - d_t > eps)  or  (no t has d_t - delta <= eps):
+// the first ("close") ends the search; the second needs one witness
+// ("touch").  Triangles farther than delta + eps can be neither; once a
+// witness is found, only triangles nearer than delta - eps still matter.
+// Both radii carry a margin, so the skips (cells by box, entries by bounding
+// sphere) never drop a triangle that could change the answer.
+__device__ bool shrink_step(const View& S, V3 q, float delta, float eps) {
+  const float m = margin(q, S.h);
+  const float r_touch = (delta + eps) * 1.0001f + m;
+  const float r_close = fmaxf(delta - eps, 0.f) * 1.0001f + m;
+  bool touch = false, close = false;
+  walk_cells(S, q, r_touch, [&](int64_t cell, float box_d2) {
+    const float lim = touch ? r_close : r_touch;
+    if (box_d2 > lim * lim) return false;
+    const uint32_t e0 = S.start[cell], e1 = S.start[cell + 1];
+    for (uint32_t e = e0; e < e1; ++e) {
+      const float4 b = S.bound[e];
+      const float l = ((touch ? r_close : r_touch) + b.w) * 1.00002f;
+      if (centre_d2(q, b) > l * l) continue;
+      const float d = entry_dist(S, q, e);
+      if (__fsub_rn(delta, d) > eps) {
+        close = true;
+        return true;
+      }
+      if (__fsub_rn(d, delta) <= eps) touch = true;
+    }
+    return false;
+  });
+  return close || !touch;
 }
 
 // ---- scene build -----------------------------------------------------------
@@ -369,12 +428,24 @@ __global__ void scan_add(uint32_t* out, int64_t n, const uint32_t* __restrict__ 
 
 __global__ void fill_kernel(View S, const float* __restrict__ pos,
                             const int32_t* __restrict__ faces, int64_t nf, uint32_t* cursor,
-                            float4* tris) {
+                            float4* tris, float4* bound) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nf) return;
   int a[3], b[3];
   float4 cr[3];
   tri_cells(S, pos, faces, t, a, b, cr);
+  // bounding sphere about the centroid, grown past its own rounding
+  const float cx = (cr[0].x + cr[1].x + cr[2].x) / 3.f, cy = (cr[0].y + cr[1].y + cr[2].y) / 3.f,
+              cz = (cr[0].z + cr[1].z + cr[2].z) / 3.f;
+  float r2 = 0.f;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float dx = cr[j].x - cx, dy = cr[j].y - cy, dz = cr[j].z - cz;
+    r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+  }
+  const float rad = sqrtf(r2) * 1.0001f +
+                    1e-5f * (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + S.h);
+  const float4 sphere = make_float4(cx, cy, cz, rad);
   for (int z = a[2]; z <= b[2]; ++z)
     for (int y = a[1]; y <= b[1]; ++y)
       for (int x = a[0]; x <= b[0]; ++x) {
@@ -382,6 +453,7 @@ __global__ void fill_kernel(View S, const float* __restrict__ pos,
         tris[3 * (int64_t)e] = cr[0];
         tris[3 * (int64_t)e + 1] = cr[1];
         tris[3 * (int64_t)e + 2] = cr[2];
+        bound[e] = sphere;
       }
 }
 
@@ -409,7 +481,7 @@ __global__ void distance_kernel(View S, const float* __restrict__ pts, int64_t n
   float r = S.h;
   float best;
   for (;;) {
-    best = bounded_min(S, q, search_radius(r, q, S.h), false, 0.f, 0.f);
+    best = nearest(S, q, r * 1.0001f + margin(q, S.h));
     if (best <= r || r >= rmax) break;
     r = fminf(r * 4.f, rmax);
   }
@@ -456,10 +528,7 @@ __global__ void __launch_bounds__(kThreads) deltas_iter(View S, const float* __r
                   __fadd_rn(v[i * C + 1], __fmul_rn(delta, o[4])),
                   __fadd_rn(v[i * C + 2], __fmul_rn(delta, o[5]))};
     bool shrink = false;
-    if (finite3(q)) {
-      const float D = bounded_min(S, q, search_radius(delta + eps, q, S.h), true, delta, eps);
-      shrink = D < 0.f || fabsf(__fsub_rn(delta, D)) > eps;
-    }
+    if (finite3(q)) shrink = shrink_step(S, q, delta, eps);
     float s = step[i];
     if (shrink) s = __fmul_rn(s, 0.5f);
     nd = shrink ? __fsub_rn(delta, s) : __fadd_rn(delta, s);
@@ -483,6 +552,7 @@ inline View view(const MplScene* s) {
   v.h = s->h;
   v.start = s->start;
   v.tris = s->tris;
+  v.bound = s->bound;
   return v;
 }
 
@@ -576,6 +646,7 @@ extern "C" int mpl_scene_create(const float* positions_dev, int64_t n_positions,
     cudaFree(total);
     cudaFree(sc->start);
     cudaFree(sc->tris);
+    cudaFree(sc->bound);
     delete sc;
     return MPL_ERR_CUDA;
   };
@@ -606,13 +677,15 @@ extern "C" int mpl_scene_create(const float* positions_dev, int64_t n_positions,
   if ((e = cudaMalloc(&sc->tris, sizeof(float4) * 3 * (total_h > 0 ? total_h : 1))) !=
       cudaSuccess)
     return fail(e);
+  if ((e = cudaMalloc(&sc->bound, sizeof(float4) * (total_h > 0 ? total_h : 1))) != cudaSuccess)
+    return fail(e);
   // counts becomes the fill cursor
   if ((e = cudaMemcpyAsync(counts, sc->start, sizeof(uint32_t) * cells, cudaMemcpyDeviceToDevice,
                            s)) != cudaSuccess)
     return fail(e);
   v = view(sc);
   fill_kernel<<<blocks(n_faces), kThreads, 0, s>>>(v, positions_dev, faces_dev, n_faces, counts,
-                                                   sc->tris);
+                                                   sc->tris, sc->bound);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail(e);
   cudaFree(counts);
@@ -626,6 +699,7 @@ extern "C" int mpl_scene_destroy(MplScene* scene) {
   if (!scene) return MPL_OK;
   cudaFree(scene->start);
   cudaFree(scene->tris);
+  cudaFree(scene->bound);
   delete scene;
   return MPL_OK;
 }

@@ -10,13 +10,21 @@ Adam at lr 1e-4 and the best-loss state after a warm-up kept.  Here every
 step runs on ``ResidualTrainer`` (hand-written forward, loss, double
 backward and Adam) and the residual batches on the batch kernel; only the
 best-loss check reads the loss back, every ``check_every`` steps.
+
+The residual stages can size their band as the reference scripts do
+(experiment_scripts/train_sdf_on_neighborhood.py:165-185 and
+train_sdf_on_neighborhood_fine.py:159-183): max_dist = max |f_frozen(v)|
+over the vertices, batch delta = 1.3 max_dist, and, with the neighbourhood
+option, per-vertex deltas from ``calc_deltas`` on the mesh's scene with
+max_delta = max_dist (medium) or 1.3 max_dist (fine).
 """
 
 from __future__ import annotations
 
 import torch
 
-from .model import SIREN
+from .model import SIREN, level_forward
+from .scene import calc_deltas
 from .train import ResidualTrainer, create_training_data_on_neighborhood
 
 
@@ -68,16 +76,45 @@ def train_coarse(surface, pool_x, pool_sdf, steps, batch, width=256, depth=3, w0
     return model, history
 
 
+def frozen_max_dist(frozen, vertices):
+    """max |sum of the frozen levels| over the vertices [M, >= 3] (a 0-d
+    float32 tensor on their device), as the reference scripts compute it
+    with the frozen models under no_grad."""
+    x = vertices[:, :3].contiguous()
+    S = None
+    for i, m in enumerate(frozen):
+        S = level_forward(m, x, S, accumulate=i > 0)
+    return S.abs().max()
+
+
 def train_residual(surface, frozen, steps, batch, delta, width=256, depth=3, w0=30,
-                   precision="bf16", seed=0, check_every=50, warmup_frac=0.1, log=None):
+                   precision="bf16", seed=0, check_every=50, warmup_frac=0.1, log=None,
+                   scene=None, neighborhood_delta=False, fine=False):
     """A residual level against the frozen ``frozen`` levels, on batches of
-    create_training_data_on_neighborhood with neighbourhood ``delta``."""
+    create_training_data_on_neighborhood with neighbourhood ``delta``.
+
+    ``delta=None`` takes 1.3 max |f_frozen(v)| over the surface rows.  With
+    ``neighborhood_delta`` the surface rows must be the vertices of the mesh
+    in ``scene`` (a ``scene.RaycastingScene``); each gets its calc_deltas
+    radius (max_delta = max_dist, or 1.3 max_dist when ``fine``) and the
+    batches use it.  Returns (model, loss history)."""
     dev = surface.device
+    max_dist = None
+    if delta is None or neighborhood_delta:
+        max_dist = frozen_max_dist(frozen, surface)
+    if delta is None:
+        delta = float(max_dist * 1.3)
+    if neighborhood_delta:
+        if scene is None:
+            raise ValueError("neighborhood_delta needs the mesh's scene")
+        surface = calc_deltas(surface[:, :6], scene, max_delta=max_dist * 1.3 if fine else max_dist,
+                              n_iters=100)
     model = _new_level(width, depth, w0, precision, dev, seed)
     tr = ResidualTrainer(model, list(frozen), lr=1e-4, precision=precision)
 
     def batch_fn(step):
         return create_training_data_on_neighborhood(surface, batch, device=dev, delta=delta,
+                                                    use_neigh_delta=neighborhood_delta,
                                                     seed=seed * 1000003 + step)["on_surf"]
 
     history = _run(tr, batch_fn, steps, check_every, warmup_frac, log)
@@ -86,16 +123,22 @@ def train_residual(surface, frozen, steps, batch, delta, width=256, depth=3, w0=
 
 def train_three_levels(surface, pool_x, pool_sdf, steps=(4000, 2000, 2000), batch=1 << 16,
                        deltas=(0.05, 0.01), width=256, depth=3, w0=30, precision="bf16", seed=0,
-                       check_every=50, log=None):
+                       check_every=50, log=None, scene=None, neighborhood_delta=False):
     """Coarse (true_sdf), medium (residual, delta0) and fine (residual,
-    delta1) levels; returns the three models and their loss histories."""
+    delta1) levels; returns the three models and their loss histories.
+    ``deltas=(None, None)`` sizes the bands from the frozen levels' error as
+    the reference scripts do; ``scene`` + ``neighborhood_delta`` add the
+    per-vertex calc_deltas radii (``surface`` then holds the mesh's vertices
+    and normals)."""
     coarse, h0 = train_coarse(surface, pool_x, pool_sdf, steps[0], batch, width, depth, w0,
                               precision, seed, check_every, log=log)
     coarse.eval()
     medium, h1 = train_residual(surface, [coarse], steps[1], batch, deltas[0], width, depth, w0,
-                                precision, seed + 1, check_every, log=log)
+                                precision, seed + 1, check_every, log=log, scene=scene,
+                                neighborhood_delta=neighborhood_delta)
     medium.eval()
     fine, h2 = train_residual(surface, [coarse, medium], steps[2], batch, deltas[1], width, depth,
-                              w0, precision, seed + 2, check_every, log=log)
+                              w0, precision, seed + 2, check_every, log=log, scene=scene,
+                              neighborhood_delta=neighborhood_delta, fine=True)
     fine.eval()
     return [coarse, medium, fine], [h0, h1, h2]
