@@ -24,9 +24,9 @@
 // visits the cells within a radius R of q in shells of growing Chebyshev
 // distance from q's cell, skipping cells whose box is farther than R.
 //
-// Decision of one bisection step (shrink_step): |delta - D| > eps for the
+// Decision of one bisection step (shrink_step_warp): |delta - D| > eps for the
 // minimum D is rewritten as "some triangle nearer than delta - eps, or none
-// within delta + eps" (exact in float32, see shrink_step), so the search
+// within delta + eps" (exact in float32, see shrink_step_warp), so the search
 // stops at the first near triangle and, once one triangle within delta + eps
 // is found, ignores everything beyond delta - eps.  The result equals the
 // brute-force minimum's comparison bit for bit.
@@ -230,29 +230,69 @@ __device__ float nearest(const View& S, V3 q, float R) {
 // witness is found, only triangles nearer than delta - eps still matter.
 // Both radii carry a margin, so the skips (cells by box, entries by bounding
 // sphere) never drop a triangle that could change the answer.
-__device__ bool shrink_step(const View& S, V3 q, float delta, float eps) {
+//
+// One query per warp: the lanes take the cells of the search box 32 at a
+// time; a warp prefix sum over the cells' entry counts hands the entries out
+// one per lane, so every lane has work while the cells have entries; the
+// close/touch flags are combined with __any_sync (they do not depend on the
+// visiting order).
+__device__ bool shrink_step_warp(const View& S, V3 q, float delta, float eps, int lane) {
   const float m = margin(q, S.h);
   const float r_touch = (delta + eps) * 1.0001f + m;
   const float r_close = fmaxf(delta - eps, 0.f) * 1.0001f + m;
-  bool touch = false, close = false;
-  walk_cells(S, q, r_touch, [&](int64_t cell, float box_d2) {
+  const int x0 = cell_of(q.x - r_touch, S.lo[0], S.h, S.dim[0]);
+  const int y0 = cell_of(q.y - r_touch, S.lo[1], S.h, S.dim[1]);
+  const int z0 = cell_of(q.z - r_touch, S.lo[2], S.h, S.dim[2]);
+  const int nx = cell_of(q.x + r_touch, S.lo[0], S.h, S.dim[0]) - x0 + 1;
+  const int ny = cell_of(q.y + r_touch, S.lo[1], S.h, S.dim[1]) - y0 + 1;
+  const int nz = cell_of(q.z + r_touch, S.lo[2], S.h, S.dim[2]) - z0 + 1;
+  const int total = nx * ny * nz;
+  bool touch = false;
+  for (int base = 0; base < total; base += 32) {
     const float lim = touch ? r_close : r_touch;
-    if (box_d2 > lim * lim) return false;
-    const uint32_t e0 = S.start[cell], e1 = S.start[cell + 1];
-    for (uint32_t e = e0; e < e1; ++e) {
-      const float4 b = S.bound[e];
-      const float l = ((touch ? r_close : r_touch) + b.w) * 1.00002f;
-      if (centre_d2(q, b) > l * l) continue;
-      const float d = entry_dist(S, q, e);
-      if (__fsub_rn(delta, d) > eps) {
-        close = true;
-        return true;
+    const int k = base + lane;
+    uint32_t e0 = 0, cnt = 0;
+    if (k < total) {
+      const int x = x0 + k % nx, y = y0 + (k / nx) % ny, z = z0 + k / (nx * ny);
+      if (cell_box_d2(S, q, x, y, z) <= lim * lim) {
+        const int64_t cell = ((int64_t)z * S.dim[1] + y) * S.dim[0] + x;
+        e0 = S.start[cell];
+        cnt = S.start[cell + 1] - e0;
       }
-      if (__fsub_rn(d, delta) <= eps) touch = true;
     }
-    return false;
-  });
-  return close || !touch;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const uint32_t T = __shfl_sync(0xffffffffu, incl, 31);
+    for (uint32_t j0 = 0; j0 < T; j0 += 32) {
+      const uint32_t j = j0 + lane;
+      // the owning cell's lane: the first lane whose inclusive count exceeds j
+      int L = 0;
+#pragma unroll
+      for (int st = 16; st; st >>= 1)
+        if (__shfl_sync(0xffffffffu, incl, L + st - 1) <= j) L += st;
+      const uint32_t oi = __shfl_sync(0xffffffffu, incl, L & 31);
+      const uint32_t oc = __shfl_sync(0xffffffffu, cnt, L & 31);
+      const uint32_t oe = __shfl_sync(0xffffffffu, e0, L & 31);
+      bool c_close = false, c_touch = false;
+      if (j < T) {
+        const uint32_t e = oe + (j - (oi - oc));
+        const float4 b = S.bound[e];
+        const float l = ((touch ? r_close : r_touch) + b.w) * 1.00002f;
+        if (centre_d2(q, b) <= l * l) {
+          const float d = entry_dist(S, q, e);
+          c_close = __fsub_rn(delta, d) > eps;
+          c_touch = __fsub_rn(d, delta) <= eps;
+        }
+      }
+      if (__any_sync(0xffffffffu, c_close)) return true;
+      touch = touch || __any_sync(0xffffffffu, c_touch);
+    }
+  }
+  return !touch;
 }
 
 // ---- scene build -----------------------------------------------------------
@@ -506,9 +546,10 @@ __global__ void deltas_init(const float* __restrict__ v, int64_t M, int C, float
   step[i] = step0;
 }
 
-// one bisection step; maxd[it] is the maximum delta before it, maxd[it + 1]
-// collects the maximum after it (zero-initialised; deltas are positive
-// whenever the loop runs, so the float bits order as integers)
+// one bisection step, one vertex per warp at a time; maxd[it] is the maximum
+// delta before it, maxd[it + 1] collects the maximum after it
+// (zero-initialised; deltas are positive whenever the loop runs, so the
+// float bits order as integers; one atomic per block)
 __global__ void __launch_bounds__(kThreads) deltas_iter(View S, const float* __restrict__ v,
                                                         int64_t M, int C, float max_delta,
                                                         float eps, float* __restrict__ out,
@@ -519,24 +560,34 @@ __global__ void __launch_bounds__(kThreads) deltas_iter(View S, const float* __r
     if (blockIdx.x == 0 && threadIdx.x == 0) maxd[it + 1] = before;
     return;
   }
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  float nd = 0.f;
-  if (i < M) {
+  __shared__ float wmax_s[kThreads / 32];
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  float wmax = 0.f;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < M; i += nwarps) {
     float* o = out + i * (C + 1);
     const float delta = o[C];
     const V3 q = {__fadd_rn(v[i * C], __fmul_rn(delta, o[3])),
                   __fadd_rn(v[i * C + 1], __fmul_rn(delta, o[4])),
                   __fadd_rn(v[i * C + 2], __fmul_rn(delta, o[5]))};
-    bool shrink = false;
-    if (finite3(q)) shrink = shrink_step(S, q, delta, eps);
+    const bool shrink = finite3(q) && shrink_step_warp(S, q, delta, eps, lane);
     float s = step[i];
     if (shrink) s = __fmul_rn(s, 0.5f);
-    nd = shrink ? __fsub_rn(delta, s) : __fadd_rn(delta, s);
-    step[i] = s;
-    o[C] = nd;
+    const float nd = shrink ? __fsub_rn(delta, s) : __fadd_rn(delta, s);
+    __syncwarp();
+    if (lane == 0) {
+      step[i] = s;
+      o[C] = nd;
+    }
+    wmax = fmaxf(wmax, nd);
   }
-  for (int off = 16; off; off >>= 1) nd = fmaxf(nd, __shfl_xor_sync(0xffffffffu, nd, off));
-  if ((threadIdx.x & 31) == 0 && nd > 0.f) atomicMax((int*)&maxd[it + 1], __float_as_int(nd));
+  if (lane == 0) wmax_s[threadIdx.x >> 5] = wmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.f;
+    for (int w = 0; w < kThreads / 32; ++w) b = fmaxf(b, wmax_s[w]);
+    if (b > 0.f) atomicMax((int*)&maxd[it + 1], __float_as_int(b));
+  }
 }
 
 __global__ void deltas_count(const float* __restrict__ maxd, int n_iters, float max_delta,
@@ -750,9 +801,12 @@ extern "C" int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev,
                                                       out_dev, step, maxd);
   MPL_LAUNCH_CHECK();
   const View v = view(scene);
+  // one warp per vertex, about 16 resident blocks per SM's worth of warps
+  const int64_t want = (n_vertices + kThreads / 32 - 1) / (kThreads / 32);
+  const unsigned nblk = (unsigned)(want < (int64_t)sm_count() * 16 ? want : (int64_t)sm_count() * 16);
   for (int it = 0; it < n_iters; ++it) {
-    deltas_iter<<<blocks(n_vertices), kThreads, 0, s>>>(v, vertices_dev, n_vertices, cols,
-                                                        max_delta, eps, out_dev, step, maxd, it);
+    deltas_iter<<<nblk, kThreads, 0, s>>>(v, vertices_dev, n_vertices, cols, max_delta, eps,
+                                          out_dev, step, maxd, it);
     MPL_LAUNCH_CHECK();
   }
   if (iterations_dev) {
