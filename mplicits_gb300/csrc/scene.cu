@@ -246,14 +246,25 @@ __device__ bool shrink_step_warp(const View& S, V3 q, float delta, float eps, in
   const int nx = cell_of(q.x + r_touch, S.lo[0], S.h, S.dim[0]) - x0 + 1;
   const int ny = cell_of(q.y + r_touch, S.lo[1], S.h, S.dim[1]) - y0 + 1;
   const int nz = cell_of(q.z + r_touch, S.lo[2], S.h, S.dim[2]) - z0 + 1;
-  const int total = nx * ny * nz;
+  const int nxy = nx * ny, total = nxy * nz;
+  const float inv_nx = 1.f / (float)nx, inv_nxy = 1.f / (float)nxy;
   bool touch = false;
   for (int base = 0; base < total; base += 32) {
     const float lim = touch ? r_close : r_touch;
     const int k = base + lane;
     uint32_t e0 = 0, cnt = 0;
     if (k < total) {
-      const int x = x0 + k % nx, y = y0 + (k / nx) % ny, z = z0 + k / (nx * ny);
+      // k -> (x, y, z) in the box: float quotients, then exact integer
+      // corrections (a step or none below 2^24 cells; no integer division)
+      int zq = (int)((float)k * inv_nxy);
+      int rem = k - zq * nxy;
+      while (rem < 0) --zq, rem += nxy;
+      while (rem >= nxy) ++zq, rem -= nxy;
+      int yq = (int)((float)rem * inv_nx);
+      int xr = rem - yq * nx;
+      while (xr < 0) --yq, xr += nx;
+      while (xr >= nx) ++yq, xr -= nx;
+      const int x = x0 + xr, y = y0 + yq, z = z0 + zq;
       if (cell_box_d2(S, q, x, y, z) <= lim * lim) {
         const int64_t cell = ((int64_t)z * S.dim[1] + y) * S.dim[0] + x;
         e0 = S.start[cell];
