@@ -231,44 +231,46 @@ __device__ float nearest(const View& S, V3 q, float R) {
 // Both radii carry a margin, so the skips (cells by box, entries by bounding
 // sphere) never drop a triangle that could change the answer.
 //
-// One query per warp: the lanes take the cells of the search box 32 at a
-// time; a warp prefix sum over the cells' entry counts hands the entries out
-// one per lane, so every lane has work while the cells have entries; the
-// close/touch flags are combined with __any_sync (they do not depend on the
-// visiting order).
+// One query per warp; the close/touch flags are combined with __any_sync
+// (they do not depend on the visiting order).
 __device__ bool shrink_step_warp(const View& S, V3 q, float delta, float eps, int lane) {
   const float m = margin(q, S.h);
   const float r_touch = (delta + eps) * 1.0001f + m;
   const float r_close = fmaxf(delta - eps, 0.f) * 1.0001f + m;
-  const int x0 = cell_of(q.x - r_touch, S.lo[0], S.h, S.dim[0]);
   const int y0 = cell_of(q.y - r_touch, S.lo[1], S.h, S.dim[1]);
   const int z0 = cell_of(q.z - r_touch, S.lo[2], S.h, S.dim[2]);
-  const int nx = cell_of(q.x + r_touch, S.lo[0], S.h, S.dim[0]) - x0 + 1;
   const int ny = cell_of(q.y + r_touch, S.lo[1], S.h, S.dim[1]) - y0 + 1;
   const int nz = cell_of(q.z + r_touch, S.lo[2], S.h, S.dim[2]) - z0 + 1;
-  const int nxy = nx * ny, total = nxy * nz;
-  const float inv_nx = 1.f / (float)nx, inv_nxy = 1.f / (float)nxy;
+  const int rows = ny * nz;
+  const float inv_ny = 1.f / (float)ny;
   bool touch = false;
-  for (int base = 0; base < total; base += 32) {
+  // Rows of cells (y, z) are contiguous in the entry lists, so the entries of
+  // the x-segment a row shares with the ball are one range: each lane takes a
+  // row, and a warp prefix sum over the ranges hands the entries out one per
+  // lane.
+  for (int base = 0; base < rows; base += 32) {
     const float lim = touch ? r_close : r_touch;
     const int k = base + lane;
     uint32_t e0 = 0, cnt = 0;
-    if (k < total) {
-      // k -> (x, y, z) in the box: float quotients, then exact integer
-      // corrections (a step or none below 2^24 cells; no integer division)
-      int zq = (int)((float)k * inv_nxy);
-      int rem = k - zq * nxy;
-      while (rem < 0) --zq, rem += nxy;
-      while (rem >= nxy) ++zq, rem -= nxy;
-      int yq = (int)((float)rem * inv_nx);
-      int xr = rem - yq * nx;
-      while (xr < 0) --yq, xr += nx;
-      while (xr >= nx) ++yq, xr -= nx;
-      const int x = x0 + xr, y = y0 + yq, z = z0 + zq;
-      if (cell_box_d2(S, q, x, y, z) <= lim * lim) {
-        const int64_t cell = ((int64_t)z * S.dim[1] + y) * S.dim[0] + x;
-        e0 = S.start[cell];
-        cnt = S.start[cell + 1] - e0;
+    if (k < rows) {
+      // k -> (y, z): a float quotient and exact integer corrections
+      int zq = (int)((float)k * inv_ny);
+      int yr = k - zq * ny;
+      while (yr < 0) --zq, yr += ny;
+      while (yr >= ny) ++zq, yr -= ny;
+      const int y = y0 + yr, z = z0 + zq;
+      const float ya = S.lo[1] + S.h * (float)y, yb = ya + S.h;
+      const float za = S.lo[2] + S.h * (float)z, zb = za + S.h;
+      const float gy = q.y < ya ? ya - q.y : (q.y > yb ? q.y - yb : 0.f);
+      const float gz = q.z < za ? za - q.z : (q.z > zb ? q.z - zb : 0.f);
+      const float w2 = lim * lim - gy * gy - gz * gz;
+      if (w2 >= 0.f) {
+        const float w = sqrtf(w2);
+        const int xa = cell_of(q.x - w, S.lo[0], S.h, S.dim[0]);
+        const int xb = cell_of(q.x + w, S.lo[0], S.h, S.dim[0]);
+        const int64_t row = ((int64_t)z * S.dim[1] + y) * S.dim[0];
+        e0 = S.start[row + xa];
+        cnt = S.start[row + xb + 1] - e0;
       }
     }
     uint32_t incl = cnt;
@@ -280,7 +282,7 @@ __device__ bool shrink_step_warp(const View& S, V3 q, float delta, float eps, in
     const uint32_t T = __shfl_sync(0xffffffffu, incl, 31);
     for (uint32_t j0 = 0; j0 < T; j0 += 32) {
       const uint32_t j = j0 + lane;
-      // the owning cell's lane: the first lane whose inclusive count exceeds j
+      // the owning row's lane: the first lane whose inclusive count exceeds j
       int L = 0;
 #pragma unroll
       for (int st = 16; st; st >>= 1)
