@@ -353,7 +353,8 @@ int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* g
  * the mean edge length when cell == 0) whose cells list the triangles that
  * overlap them.  Setup, not the hot path: mpl_scene_create synchronises
  * `stream` and allocates the scene's device memory itself (the one exception
- * to the caller-owned-memory rule; mpl_scene_destroy frees it).  positions
+ * to the caller-owned-memory rule; mpl_scene_destroy waits for the device's
+ * queued work and frees it).  positions
  * [n_positions, 3] float32, faces [n_faces, 3] int32; a face index outside
  * [0, n_positions) gives MPL_ERR_INVALID_ARG.  The scene copies the corners:
  * the inputs may be freed after the call. */

@@ -761,10 +761,16 @@ extern "C" int mpl_scene_create(const float* positions_dev, int64_t n_positions,
 
 extern "C" int mpl_scene_destroy(MplScene* scene) {
   if (!scene) return MPL_OK;
+  // queries still queued on any stream read the grid: let them finish
+  const cudaError_t e = cudaDeviceSynchronize();
   cudaFree(scene->start);
   cudaFree(scene->tris);
   cudaFree(scene->bound);
   delete scene;
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return MPL_ERR_CUDA;
+  }
   return MPL_OK;
 }
 
