@@ -8,8 +8,9 @@
  *  - Every entry point returns an int status (MPL_OK == 0); nothing throws.
  *  - All pointers named *_dev, and every array argument unless stated
  *    otherwise, are device pointers owned by the caller.  The library never
- *    allocates device memory inside a call: scratch space is caller-provided
- *    and sized by the matching *_bytes query.
+ *    allocates device memory inside a call (the one exception is the setup
+ *    call mpl_scene_create): scratch space is caller-provided and sized by
+ *    the matching *_bytes query.
  *  - `stream` is a cudaStream_t passed as void*; every launch is
  *    stream-ordered, and no call synchronises the host unless its comment
  *    says so.
