@@ -563,7 +563,7 @@ __global__ void deltas_init(const float* __restrict__ v, int64_t M, int C, float
 // delta before it, maxd[it + 1] collects the maximum after it
 // (zero-initialised; deltas are positive whenever the loop runs, so the
 // float bits order as integers; one atomic per block)
-__global__ void __launch_bounds__(kThreads) deltas_iter(View S, const float* __restrict__ v,
+__global__ void __launch_bounds__(kThreads, 5) deltas_iter(View S, const float* __restrict__ v,
                                                         int64_t M, int C, float max_delta,
                                                         float eps, float* __restrict__ out,
                                                         float* __restrict__ step, float* maxd,
