@@ -92,3 +92,18 @@ def test_arguments():
         od.calc_deltas(np.zeros((2, 5), np.float32), pos, faces)
     with pytest.raises(ValueError):
         od.calc_deltas(np.zeros((2, 6), np.float32), pos, np.array([[0, 1, 3]], np.int32))
+
+
+def test_oracle_stopping_rule_edges():
+    from golden.make_calc_deltas import slab
+    pos, nrm, faces = slab(4, 0.08)
+    V = np.concatenate([pos, nrm], 1)
+    # the first step already reaches max_delta: no iteration runs
+    out, it = od.calc_deltas(V, pos, faces, 0.2, 1)
+    assert it == 0 and np.all(out[:, 6] == np.float32(0.2))
+    out, it = od.calc_deltas(V, pos, faces, 0.0, 50)
+    assert it == 0 and np.all(out[:, 6] == 0.0)
+    # grid and brute force agree when the ball covers the whole mesh
+    a, ia = od.calc_deltas(V, pos, faces, 5.0, 30)
+    b, ib = od.calc_deltas(V, pos, faces, 5.0, 30, cell=0.05)
+    assert ia == ib and np.array_equal(a, b)

@@ -100,3 +100,46 @@ def test_scene_rejects_bad_faces_and_inputs():
     with pytest.raises(ValueError):
         calc_deltas(np.zeros((4, 5), np.float32), scene)
     assert capi.device_status() == capi.MPL_OK
+
+
+def _degenerate_mesh():
+    from golden.make_calc_deltas import slab
+    pos, nrm, faces = slab(5, 0.1)
+    extra = np.array([[0.1, 0.1, 0.05], [0.3, 0.1, 0.05], [0.2, 0.1, 0.05]], np.float32)
+    base = pos.shape[0]
+    pos = np.concatenate([pos, extra])
+    nrm = np.concatenate([nrm, np.tile([[0, 0, 1]], (3, 1)).astype(np.float32)])
+    # a zero-area triangle (collinear corners) and one with a repeated corner
+    faces = np.concatenate([faces, [[base, base + 1, base + 2], [base, base, base + 1]]])
+    return pos, nrm, faces.astype(np.int32)
+
+
+@pytest.mark.parametrize("case", ["degenerate", "huge_radius", "one_iteration", "zero_max",
+                                  "offset_scene"])
+def test_edge_cases_bit_exact(case):
+    from mplicits_gb300.scene import RaycastingScene, calc_deltas
+    from golden.make_calc_deltas import slab
+    pos, nrm, faces = slab(6, 0.08)
+    md, iters = 0.2, 100
+    if case == "degenerate":
+        pos, nrm, faces = _degenerate_mesh()
+    elif case == "huge_radius":
+        md = 5.0
+    elif case == "one_iteration":
+        iters = 1
+    elif case == "zero_max":
+        md = 0.0
+    elif case == "offset_scene":
+        pos = pos * 40.0 + np.float32([100.0, -250.0, 30.0])
+        md = 8.0
+    V = np.concatenate([pos, nrm], 1).astype(np.float32)
+    scene = RaycastingScene(pos, faces)
+    got, it = calc_deltas(V, scene, max_delta=md, n_iters=iters, return_iterations=True)
+    want, it_ref = od.calc_deltas(V, pos, faces, md, iters)
+    assert it == it_ref
+    np.testing.assert_array_equal(got.cpu().numpy(), want)
+    rng = np.random.default_rng(3)
+    pts = (pos[rng.integers(0, pos.shape[0], 500)] + rng.normal(0, 0.1, (500, 3)) *
+           (40.0 if case == "offset_scene" else 1.0)).astype(np.float32)
+    np.testing.assert_array_equal(scene.compute_distance(pts).cpu().numpy(),
+                                  od.compute_distance(pos, faces, pts))
