@@ -96,9 +96,10 @@ def calc_deltas(vertices, scene, max_delta=0.05, n_iters=100, device=None, eps=2
     scene's device: the rows with unit normals and the neighbourhood radius
     appended.  ``max_delta`` may be a float or a 0-d tensor (the reference's
     callers pass ``max |f(v)|`` as a tensor); it is used in float32, and the
-    first step is max_delta / n_iters in float32.  With
-    ``return_iterations`` also returns the number of iterations run (one
-    host read).  No host synchronisation otherwise.
+    first step is max_delta / n_iters in float32 (a device tensor is read
+    on the host once).  With ``return_iterations`` also returns the number
+    of iterations run (one more host read).  The iterations themselves run
+    without host round trips.
     """
     dev = scene.device if device is None else torch.device(device)
     V = torch.as_tensor(vertices).detach().to(dev, torch.float32).contiguous()
