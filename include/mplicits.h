@@ -358,7 +358,8 @@ int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* g
  * queued work and frees it).  positions
  * [n_positions, 3] float32, faces [n_faces, 3] int32; a face index outside
  * [0, n_positions) gives MPL_ERR_INVALID_ARG.  The scene copies the corners:
- * the inputs may be freed after the call. */
+ * the inputs may be freed after the call.  Queries must be made with the
+ * scene's device current (else MPL_ERR_INVALID_ARG). */
 typedef struct MplScene MplScene;
 int mpl_scene_create(const float* positions_dev, int64_t n_positions, const int32_t* faces_dev,
                      int64_t n_faces, float cell, MplScene** scene, void* stream);

@@ -622,6 +622,17 @@ inline View view(const MplScene* s) {
 
 inline unsigned blocks(int64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
+// queries run on the device that holds the scene's grid
+inline int check_device(const MplScene* s) {
+  int dev = -1;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return MPL_ERR_CUDA;
+  }
+  return dev == s->device ? MPL_OK : MPL_ERR_INVALID_ARG;
+}
+
 }  // namespace scene
 }  // namespace mpl
 
@@ -790,6 +801,8 @@ extern "C" int mpl_scene_compute_distance(const MplScene* scene, const float* po
                                           int64_t n, float* out_dev, void* stream) {
   if (!scene || n < 0 || (n > 0 && (!points_dev || !out_dev))) return MPL_ERR_INVALID_ARG;
   if (n == 0) return MPL_OK;
+  const int dst = check_device(scene);
+  if (dst != MPL_OK) return dst;
   const View v = view(scene);
   distance_kernel<<<blocks(n), kThreads, 0, (cudaStream_t)stream>>>(v, points_dev, n, out_dev);
   MPL_LAUNCH_CHECK();
@@ -811,6 +824,8 @@ extern "C" int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev,
       n_iters < 1 || !isfinite(max_delta) || !(eps >= 0.f))
     return MPL_ERR_INVALID_ARG;
   if (((uintptr_t)scratch_dev & 255) != 0) return MPL_ERR_INVALID_ARG;
+  const int dst = check_device(scene);
+  if (dst != MPL_OK) return dst;
   cudaStream_t s = (cudaStream_t)stream;
   float* maxd = (float*)scratch_dev;
   float* step = (float*)((char*)scratch_dev + ((n_iters + 1 + 63) / 64) * 256);

@@ -102,6 +102,10 @@ def calc_deltas(vertices, scene, max_delta=0.05, n_iters=100, device=None, eps=2
     without host round trips.
     """
     dev = scene.device if device is None else torch.device(device)
+    if dev.type != "cuda" or (dev.index if dev.index is not None else torch.cuda.current_device()) \
+            != (scene.device.index if scene.device.index is not None
+                else torch.cuda.current_device()):
+        raise ValueError(f"calc_deltas runs on the scene's device ({scene.device}), not {dev}")
     V = torch.as_tensor(vertices).detach().to(dev, torch.float32).contiguous()
     if V.dim() != 2 or V.shape[1] < 6:
         raise ValueError("calc_deltas needs vertices [M, >= 6] (xyz, normal, ...)")
