@@ -18,6 +18,11 @@ mc        ctypes wrapper of ``mc.c``: marching cubes with the derived case
           scikit-image, which is absent here: parity to scikit-image itself is
           unpinned; the GPU kernel is pinned to this restatement).
 fp64      torch FP64 evaluator used only to state the SDF error of results.
+deltas    ctypes wrapper of ``deltas.c``: calc_deltas
+          (experiment_scripts/utils.py:46-89) over an exact float32
+          nearest-triangle distance, brute force or on a uniform grid (open3d,
+          whose scene the reference queries, is absent: parity to its rounding
+          is unpinned; the loop is pinned to the reference's own code).
 
 Pinning: ``tests/golden`` holds vectors generated by importing the reference
 ``i3d`` package (``tests/golden/make_golden.py``); ``tests/test_oracle.py``
