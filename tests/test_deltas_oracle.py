@@ -107,3 +107,22 @@ def test_oracle_stopping_rule_edges():
     a, ia = od.calc_deltas(V, pos, faces, 5.0, 30)
     b, ib = od.calc_deltas(V, pos, faces, 5.0, 30, cell=0.05)
     assert ia == ib and np.array_equal(a, b)
+
+
+def test_synthetic_mesh_is_closed_and_outward():
+    """The triangulated synthetic surface: every edge shared by exactly two
+    faces in opposite directions, and face normals along the analytic
+    vertex normals."""
+    from mplicits_gb300 import synthetic
+    pos, nrm, faces = synthetic.surface_mesh(12, 18)
+    assert pos.shape == ((12 - 1) * 18 + 2, 3) and faces.shape == (2 * (12 - 1) * 18, 3)
+    e = np.concatenate([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]])
+    directed = {tuple(x) for x in e}
+    assert len(directed) == e.shape[0]
+    assert all((b, a) in directed for a, b in directed)
+    a, b, c = pos[faces[:, 0]], pos[faces[:, 1]], pos[faces[:, 2]]
+    fn = np.cross(b - a, c - a)
+    assert np.all(np.sum(fn * nrm[faces].mean(1), 1) > 0)
+    assert np.allclose(np.linalg.norm(nrm, axis=1), 1, atol=1e-6)
+    with pytest.raises(ValueError):
+        synthetic.surface_mesh(1, 18)
