@@ -524,20 +524,24 @@ def deltas_bench(device, K, W):
             "gpu_launches": K * (DELTAS_ITERS + 2)}
 
 
-def deltas_cpu_baseline(iters, n=4096):
-    """The oracle's grid search (C, all host threads) on a seeded subset of
-    the same vertices run for the GPU run's iteration count."""
+def deltas_cpu_baseline(iters, n=16384):
+    """The oracle's grid search (C, all host threads; each step decided with
+    early exits and bounding-sphere skips, as the GPU kernel does) on a
+    seeded subset of the same vertices run for the GPU run's iteration
+    count."""
     from oracle import deltas as od
     V, pos, faces = deltas_mesh()
     idx = np.random.default_rng(2).choice(V.shape[0], n, replace=False)
-    od.calc_deltas(V[idx[:64]], pos, faces, DELTAS_MAX, DELTAS_ITERS, cell=0.005,
-                   force_iters=1)  # compile and warm
+    od.calc_deltas(V[idx[:64]], pos, faces, DELTAS_MAX, DELTAS_ITERS, cell=0.02,
+                   force_iters=1, fast=True)  # compile and warm
     t0 = time.perf_counter()
-    od.calc_deltas(V[idx], pos, faces, DELTAS_MAX, DELTAS_ITERS, cell=0.005, force_iters=iters)
+    od.calc_deltas(V[idx], pos, faces, DELTAS_MAX, DELTAS_ITERS, cell=0.02, force_iters=iters,
+                   fast=True)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "vertices/s", "cores": os.cpu_count() or 1, "kind": "port",
-            "sample": f"{n} of the {V.shape[0]} vertices, {iters} iterations, grid cell 0.005, "
-                      "grid build included (C, OpenMP over vertices)"}
+            "sample": f"{n} of the {V.shape[0]} vertices, {iters} iterations, grid cell 0.02, "
+                      "close/touch decision with bounding-sphere skips, grid build included "
+                      "(C, OpenMP over vertices)"}
 
 
 # first step of the persistent marching launch (tensor-core precisions): from

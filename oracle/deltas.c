@@ -194,16 +194,73 @@ static float grid_min(const Grid* g, const float* q, float R, const float* pos,
   return best;
 }
 
+/* The comparison |delta - D| > eps for D the minimum over all triangles,
+ * decided as (some triangle with delta - d > eps) or (no triangle with
+ * d - delta <= eps): the rounded differences are monotone in d, so both
+ * forms agree.  Triangles whose bounding sphere (centroid, grown radius)
+ * lies beyond delta + eps plus a margin can be neither; once a triangle with
+ * d - delta <= eps is found, only those nearer than delta - eps still
+ * matter; the search stops at the first triangle with delta - d > eps.  The
+ * same answer as the minimum, with far fewer distance evaluations. */
+static int decide_fast(const Grid* g, const float* sph, const float* q, float delta, float eps,
+                       const float* pos, const int32_t* faces) {
+  const float m = 1e-5f * (fmaxf(fabsf(q[0]), fmaxf(fabsf(q[1]), fabsf(q[2]))) + g->h);
+  const float r_touch = (delta + eps) * 1.0001f + m;
+  const float r_close = fmaxf(delta - eps, 0.f) * 1.0001f + m;
+  int64_t a[3], b[3];
+  for (int k = 0; k < 3; ++k) {
+    a[k] = cell_of(q[k] - r_touch, g->lo[k], g->h, g->dim[k]);
+    b[k] = cell_of(q[k] + r_touch, g->lo[k], g->h, g->dim[k]);
+  }
+  int touch = 0;
+  for (int64_t z = a[2]; z <= b[2]; ++z)
+    for (int64_t y = a[1]; y <= b[1]; ++y)
+      for (int64_t x = a[0]; x <= b[0]; ++x) {
+        const int64_t c = (z * g->dim[1] + y) * g->dim[0] + x;
+        for (int64_t i = g->start[c]; i < g->start[c + 1]; ++i) {
+          const int64_t t = g->tri[i];
+          const float* s4 = sph + 4 * t;
+          const float l = ((touch ? r_close : r_touch) + s4[3]) * 1.00002f;
+          const float dx = q[0] - s4[0], dy = q[1] - s4[1], dz = q[2] - s4[2];
+          if (dx * dx + dy * dy + dz * dz > l * l) continue;
+          const float d = sqrtf(tri_dist2(q, vtx(pos, faces, t, 0), vtx(pos, faces, t, 1),
+                                          vtx(pos, faces, t, 2)));
+          if (delta - d > eps) return 1;
+          if (d - delta <= eps) touch = 1;
+        }
+      }
+  return !touch;
+}
+
+static float* spheres(const float* pos, const int32_t* faces, int64_t T, float h) {
+  float* s = (float*)malloc(sizeof(float) * 4 * (size_t)(T > 0 ? T : 1));
+  for (int64_t t = 0; t < T; ++t) {
+    const float *p0 = vtx(pos, faces, t, 0), *p1 = vtx(pos, faces, t, 1),
+                *p2 = vtx(pos, faces, t, 2);
+    float c[3], r2 = 0.f;
+    for (int k = 0; k < 3; ++k) c[k] = (p0[k] + p1[k] + p2[k]) / 3.f;
+    const float* p[3] = {p0, p1, p2};
+    for (int j = 0; j < 3; ++j) {
+      const float dx = p[j][0] - c[0], dy = p[j][1] - c[1], dz = p[j][2] - c[2];
+      r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+    }
+    s[4 * t] = c[0], s[4 * t + 1] = c[1], s[4 * t + 2] = c[2];
+    s[4 * t + 3] = sqrtf(r2) * 1.0001f + 1e-5f * (fmaxf(fabsf(c[0]), fmaxf(fabsf(c[1]), fabsf(c[2]))) + h);
+  }
+  return s;
+}
+
 /* Runs calc_deltas on M vertices of C >= 6 columns (xyz, normal, ...),
  * writing [M, C + 1] rows (normal normalised, delta appended) to out.
- * cell <= 0: brute-force distances; cell > 0: a grid with that cell side.
+ * cell <= 0: brute-force distances; cell > 0: a grid with that cell side
+ * (fast != 0: decide_fast on it, else the minimum over the cells in range).
  * force_iters >= 0 runs exactly that many iterations whatever the maximum
  * (to check a subset of a larger run, whose stopping point the whole set
  * decided).  Returns the number of iterations run, or -1 on an argument
  * error. */
 int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* pos, int64_t nv,
                            const int32_t* faces, int64_t T, float max_delta, int n_iters,
-                           float eps, float cell, int force_iters, float* out) {
+                           float eps, float cell, int force_iters, int fast, float* out) {
   if (M <= 0 || C < 6 || n_iters < 1) return -1;
   const int64_t W = C + 1;
   const float step0 = max_delta / (float)n_iters;
@@ -224,6 +281,7 @@ int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* po
     free(step);
     return -1;
   }
+  float* sph = cell > 0.f && fast ? spheres(pos, faces, T, cell) : NULL;
   float maxd = step0;
   int it = 0;
   while (force_iters >= 0 ? it < force_iters : (it < n_iters && maxd < max_delta)) {
@@ -235,7 +293,9 @@ int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* po
       float q[3];
       for (int k = 0; k < 3; ++k) q[k] = verts[i * C + k] + delta * o[3 + k];
       int shrink = 0;
-      if (finite3(q)) {
+      if (finite3(q) && sph) {
+        shrink = decide_fast(&g, sph, q, delta, eps, pos, faces);
+      } else if (finite3(q)) {
         float D;
         if (cell > 0.f) {
           const float R = (delta + eps) * 1.0001f +
@@ -257,6 +317,7 @@ int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* po
     ++it;
   }
   free(step);
+  free(sph);
   free(g.start);
   free(g.tri);
   return it;

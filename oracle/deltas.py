@@ -43,7 +43,8 @@ def _load():
         lib.mpl_oracle_tri_dist.restype = F
         lib.mpl_oracle_compute_distance.argtypes = [P, P, I64, P, I64, P]
         lib.mpl_oracle_calc_deltas.argtypes = [P, I64, ctypes.c_int, P, I64, P, I64, F,
-                                               ctypes.c_int, F, F, ctypes.c_int, P]
+                                               ctypes.c_int, F, F, ctypes.c_int, ctypes.c_int,
+                                               P]
         lib.mpl_oracle_calc_deltas.restype = ctypes.c_int
         _lib = lib
     return _lib
@@ -79,13 +80,15 @@ def compute_distance(positions, faces, points):
 
 
 def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-4, cell=0.0,
-                force_iters=None):
+                force_iters=None, fast=False):
     """The reference's calc_deltas: returns ([M, C + 1] float32 rows, the
     number of iterations run).  ``cell`` > 0 searches a uniform grid of that
     cell side instead of every triangle (same result).  ``force_iters`` runs
     exactly that many iterations (each vertex's path depends on the others
     only through the stopping point, so a subset of a larger run is checked
-    with the larger run's iteration count)."""
+    with the larger run's iteration count).  ``fast`` (with ``cell`` > 0)
+    decides each step with early exits and bounding-sphere skips instead of
+    the minimum (same result; the timed CPU baseline uses it)."""
     V = np.ascontiguousarray(vertices, np.float32)
     M, C = V.shape
     if M == 0:
@@ -97,7 +100,7 @@ def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-
                                         fc.shape[0], float(np.float32(max_delta)), int(n_iters),
                                         float(np.float32(eps)), float(cell),
                                         -1 if force_iters is None else int(force_iters),
-                                        _ptr(out))
+                                        1 if fast else 0, _ptr(out))
     if it < 0:
         raise ValueError("calc_deltas: bad arguments (needs C >= 6 columns and n_iters >= 1)")
     return out, it

@@ -17,11 +17,12 @@ def _golden():
         yield str(name), {k.split("__", 1)[1]: g[k] for k in g.files if k.startswith(f"{name}__")}
 
 
-@pytest.mark.parametrize("cell", [0.0, 0.03, 0.11])
-def test_oracle_equals_reference_loop(cell):
+@pytest.mark.parametrize("cell,fast", [(0.0, False), (0.03, False), (0.11, False),
+                                       (0.03, True), (0.11, True), (0.004, True)])
+def test_oracle_equals_reference_loop(cell, fast):
     for name, c in _golden():
         out, it = od.calc_deltas(c["vertices"], c["positions"], c["faces"], c["max_delta"],
-                                 int(c["n_iters"]), cell=cell)
+                                 int(c["n_iters"]), cell=cell, fast=fast)
         assert it == int(c["iterations"]), name
         np.testing.assert_array_equal(out, c["out"], err_msg=name)
 
@@ -126,3 +127,12 @@ def test_synthetic_mesh_is_closed_and_outward():
     assert np.allclose(np.linalg.norm(nrm, axis=1), 1, atol=1e-6)
     with pytest.raises(ValueError):
         synthetic.surface_mesh(1, 18)
+
+
+def test_fast_decision_equals_minimum_on_a_larger_mesh():
+    from mplicits_gb300 import synthetic
+    pos, nrm, faces = synthetic.surface_mesh(40, 80)
+    V = np.concatenate([pos, nrm], 1)
+    a, ia = od.calc_deltas(V, pos, faces, 0.06, 100, cell=0.03)
+    b, ib = od.calc_deltas(V, pos, faces, 0.06, 100, cell=0.02, fast=True)
+    assert ia == ib and np.array_equal(a, b)
