@@ -250,10 +250,152 @@ static float* spheres(const float* pos, const int32_t* faces, int64_t T, float h
   return s;
 }
 
+/* ---- bounding-volume hierarchy: triangles sorted by the Morton code of
+ * their centroid (10 bits per axis over the mesh box), then split at the
+ * middle of each index range down to leaves of <= 4; node boxes are the
+ * exact float min/max of their triangles' corners ---- */
+typedef struct {
+  float lo[3], hi[3];
+  int32_t left, right; /* children (internal) */
+  int32_t first, count; /* triangle range in order[] (leaf: count > 0) */
+} BNode;
+
+typedef struct {
+  BNode* nodes;
+  int32_t* order;
+  int32_t n;
+} Bvh;
+
+static uint32_t spread10(uint32_t v) {
+  v &= 1023u;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+static const uint32_t* g_codes; /* qsort key (the build is single-threaded) */
+static int by_code(const void* a, const void* b) {
+  const uint32_t x = g_codes[*(const int32_t*)a], y = g_codes[*(const int32_t*)b];
+  if (x != y) return x < y ? -1 : 1;
+  return *(const int32_t*)a - *(const int32_t*)b;
+}
+
+static int32_t bvh_node(Bvh* h, const float* pos, const int32_t* faces, int32_t first,
+                        int32_t count) {
+  const int32_t id = h->n++;
+  BNode* nd = &h->nodes[id];
+  if (count <= 4) {
+    nd->first = first, nd->count = count, nd->left = nd->right = -1;
+    for (int k = 0; k < 3; ++k) nd->lo[k] = INFINITY, nd->hi[k] = -INFINITY;
+    for (int32_t i = first; i < first + count; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const float x = vtx(pos, faces, h->order[i], j)[k];
+          nd->lo[k] = fminf(nd->lo[k], x);
+          nd->hi[k] = fmaxf(nd->hi[k], x);
+        }
+    return id;
+  }
+  const int32_t half = count / 2;
+  const int32_t l = bvh_node(h, pos, faces, first, half);
+  const int32_t r = bvh_node(h, pos, faces, first + half, count - half);
+  nd = &h->nodes[id];
+  nd->left = l, nd->right = r, nd->first = 0, nd->count = 0;
+  for (int k = 0; k < 3; ++k) {
+    nd->lo[k] = fminf(h->nodes[l].lo[k], h->nodes[r].lo[k]);
+    nd->hi[k] = fmaxf(h->nodes[l].hi[k], h->nodes[r].hi[k]);
+  }
+  return id;
+}
+
+static int bvh_build(Bvh* h, const float* pos, int64_t nv, const int32_t* faces, int64_t T) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < nv; ++i)
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = fminf(lo[k], pos[3 * i + k]);
+      hi[k] = fmaxf(hi[k], pos[3 * i + k]);
+    }
+  uint32_t* codes = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)T);
+  h->order = (int32_t*)malloc(sizeof(int32_t) * (size_t)T);
+  h->nodes = (BNode*)malloc(sizeof(BNode) * (size_t)(2 * T + 1));
+  h->n = 0;
+  if (!codes || !h->order || !h->nodes) return -1;
+  for (int64_t t = 0; t < T; ++t) {
+    uint32_t c = 0;
+    for (int k = 0; k < 3; ++k) {
+      const float cen = (vtx(pos, faces, t, 0)[k] + vtx(pos, faces, t, 1)[k] +
+                         vtx(pos, faces, t, 2)[k]) / 3.f;
+      const float ext = hi[k] - lo[k];
+      float u = ext > 0.f ? (cen - lo[k]) / ext : 0.f;
+      if (!(u >= 0.f)) u = 0.f; /* NaN corners map to 0 */
+      if (u > 1.f) u = 1.f;
+      c |= spread10((uint32_t)(u * 1023.f)) << k;
+    }
+    codes[t] = c;
+    h->order[t] = (int32_t)t;
+  }
+  g_codes = codes;
+  qsort(h->order, (size_t)T, sizeof(int32_t), by_code);
+  free(codes);
+  bvh_node(h, pos, faces, 0, (int32_t)T);
+  return 0;
+}
+
+static float box_d2(const float* lo, const float* hi, const float* q) {
+  float s = 0.f;
+  for (int k = 0; k < 3; ++k) {
+    const float g = q[k] < lo[k] ? lo[k] - q[k] : (q[k] > hi[k] ? q[k] - hi[k] : 0.f);
+    s += g * g;
+  }
+  return s;
+}
+
+/* decide_fast's close/touch decision over the hierarchy, nearer child first */
+static int decide_bvh(const Bvh* h, const float* q, float delta, float eps, const float* pos,
+                      const int32_t* faces) {
+  const float m = 1e-5f * (fmaxf(fabsf(q[0]), fmaxf(fabsf(q[1]), fabsf(q[2]))) + delta);
+  const float r_touch = (delta + eps) * 1.0001f + m;
+  const float r_close = fmaxf(delta - eps, 0.f) * 1.0001f + m;
+  int32_t stack[128];
+  int sp = 0, touch = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const BNode* nd = &h->nodes[stack[--sp]];
+    const float lim = touch ? r_close : r_touch;
+    if (box_d2(nd->lo, nd->hi, q) > lim * lim) continue;
+    if (nd->count > 0) {
+      for (int32_t i = nd->first; i < nd->first + nd->count; ++i) {
+        const int32_t t = h->order[i];
+        const float d = sqrtf(tri_dist2(q, vtx(pos, faces, t, 0), vtx(pos, faces, t, 1),
+                                        vtx(pos, faces, t, 2)));
+        if (delta - d > eps) return 1;
+        if (d - delta <= eps) touch = 1;
+      }
+      continue;
+    }
+    const float dl = box_d2(h->nodes[nd->left].lo, h->nodes[nd->left].hi, q);
+    const float dr = box_d2(h->nodes[nd->right].lo, h->nodes[nd->right].hi, q);
+    /* push the farther child first so the nearer one is visited next */
+    /* midpoint splits keep the depth <= 31 for T < 2^30: the stack never
+       holds more than depth + 2 entries */
+    if (dl <= dr) {
+      stack[sp++] = nd->right;
+      stack[sp++] = nd->left;
+    } else {
+      stack[sp++] = nd->left;
+      stack[sp++] = nd->right;
+    }
+  }
+  return !touch;
+}
+
 /* Runs calc_deltas on M vertices of C >= 6 columns (xyz, normal, ...),
  * writing [M, C + 1] rows (normal normalised, delta appended) to out.
  * cell <= 0: brute-force distances; cell > 0: a grid with that cell side
- * (fast != 0: decide_fast on it, else the minimum over the cells in range).
+ * (fast == 1: decide_fast on it, else the minimum over the cells in range);
+ * fast == 2: decide_bvh on a hierarchy (cell unused).
  * force_iters >= 0 runs exactly that many iterations whatever the maximum
  * (to check a subset of a larger run, whose stopping point the whole set
  * decided).  Returns the number of iterations run, or -1 on an argument
@@ -281,7 +423,15 @@ int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* po
     free(step);
     return -1;
   }
-  float* sph = cell > 0.f && fast ? spheres(pos, faces, T, cell) : NULL;
+  float* sph = cell > 0.f && fast == 1 ? spheres(pos, faces, T, cell) : NULL;
+  Bvh bvh;
+  memset(&bvh, 0, sizeof bvh);
+  if (fast == 2 && (T >= (int64_t)1 << 30 || bvh_build(&bvh, pos, nv, faces, T) != 0)) {
+    free(step);
+    free(bvh.nodes);
+    free(bvh.order);
+    return -1;
+  }
   float maxd = step0;
   int it = 0;
   while (force_iters >= 0 ? it < force_iters : (it < n_iters && maxd < max_delta)) {
@@ -293,7 +443,9 @@ int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* po
       float q[3];
       for (int k = 0; k < 3; ++k) q[k] = verts[i * C + k] + delta * o[3 + k];
       int shrink = 0;
-      if (finite3(q) && sph) {
+      if (finite3(q) && fast == 2) {
+        shrink = decide_bvh(&bvh, q, delta, eps, pos, faces);
+      } else if (finite3(q) && sph) {
         shrink = decide_fast(&g, sph, q, delta, eps, pos, faces);
       } else if (finite3(q)) {
         float D;
@@ -318,6 +470,8 @@ int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* po
   }
   free(step);
   free(sph);
+  free(bvh.nodes);
+  free(bvh.order);
   free(g.start);
   free(g.tri);
   return it;

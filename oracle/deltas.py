@@ -80,7 +80,7 @@ def compute_distance(positions, faces, points):
 
 
 def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-4, cell=0.0,
-                force_iters=None, fast=False):
+                force_iters=None, fast=False, bvh=False):
     """The reference's calc_deltas: returns ([M, C + 1] float32 rows, the
     number of iterations run).  ``cell`` > 0 searches a uniform grid of that
     cell side instead of every triangle (same result).  ``force_iters`` runs
@@ -88,7 +88,9 @@ def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-
     only through the stopping point, so a subset of a larger run is checked
     with the larger run's iteration count).  ``fast`` (with ``cell`` > 0)
     decides each step with early exits and bounding-sphere skips instead of
-    the minimum (same result; the timed CPU baseline uses it)."""
+    the minimum (same result).  ``bvh`` decides the same way over a
+    bounding-volume hierarchy instead of a grid (``cell`` unused; the timed
+    CPU baseline uses it: open3d's scene is a hierarchy too)."""
     V = np.ascontiguousarray(vertices, np.float32)
     M, C = V.shape
     if M == 0:
@@ -100,7 +102,7 @@ def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-
                                         fc.shape[0], float(np.float32(max_delta)), int(n_iters),
                                         float(np.float32(eps)), float(cell),
                                         -1 if force_iters is None else int(force_iters),
-                                        1 if fast else 0, _ptr(out))
+                                        2 if bvh else (1 if fast else 0), _ptr(out))
     if it < 0:
         raise ValueError("calc_deltas: bad arguments (needs C >= 6 columns and n_iters >= 1)")
     return out, it

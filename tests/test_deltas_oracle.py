@@ -17,12 +17,14 @@ def _golden():
         yield str(name), {k.split("__", 1)[1]: g[k] for k in g.files if k.startswith(f"{name}__")}
 
 
-@pytest.mark.parametrize("cell,fast", [(0.0, False), (0.03, False), (0.11, False),
-                                       (0.03, True), (0.11, True), (0.004, True)])
-def test_oracle_equals_reference_loop(cell, fast):
+@pytest.mark.parametrize("cell,fast,bvh", [(0.0, False, False), (0.03, False, False),
+                                           (0.11, False, False), (0.03, True, False),
+                                           (0.11, True, False), (0.004, True, False),
+                                           (0.0, False, True)])
+def test_oracle_equals_reference_loop(cell, fast, bvh):
     for name, c in _golden():
         out, it = od.calc_deltas(c["vertices"], c["positions"], c["faces"], c["max_delta"],
-                                 int(c["n_iters"]), cell=cell, fast=fast)
+                                 int(c["n_iters"]), cell=cell, fast=fast, bvh=bvh)
         assert it == int(c["iterations"]), name
         np.testing.assert_array_equal(out, c["out"], err_msg=name)
 
@@ -135,4 +137,5 @@ def test_fast_decision_equals_minimum_on_a_larger_mesh():
     V = np.concatenate([pos, nrm], 1)
     a, ia = od.calc_deltas(V, pos, faces, 0.06, 100, cell=0.03)
     b, ib = od.calc_deltas(V, pos, faces, 0.06, 100, cell=0.02, fast=True)
-    assert ia == ib and np.array_equal(a, b)
+    c, ic = od.calc_deltas(V, pos, faces, 0.06, 100, bvh=True)
+    assert ia == ib == ic and np.array_equal(a, b) and np.array_equal(a, c)
