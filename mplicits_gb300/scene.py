@@ -78,7 +78,8 @@ class RaycastingScene:
 
     def _release(self):
         if self._handle is not None:
-            capi.load().mpl_scene_destroy(self._handle)
+            with torch.cuda.device(self.device):
+                capi.load().mpl_scene_destroy(self._handle)
             self._handle = None
 
     def __del__(self):
