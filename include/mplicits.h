@@ -159,6 +159,12 @@ int mpl_level_gradient(const MplNet* net, const void* packed_dev, const MplPoint
 int mpl_band_compact(const float* S_dev, const int32_t* index_dev, const int32_t* n_dev,
                      int64_t n, const MplBand* band, void* stream);
 
+/* max_j |S[j]| over S[0 .. n) into *out_dev (device float; 0 for n = 0, NaN
+ * if any S[j] is NaN), stream-ordered, no host sync.  Replaces the per-chunk
+ * `float(s.abs().max())` of adaptive_deltas (reconstruct.py:28-31), which
+ * reads every chunk's maximum back to the host. */
+int mpl_abs_max(const float* S_dev, int64_t n, float* out_dev, void* stream);
+
 /* ---- marching cubes (i3d/meshing.py:267-313; scikit-image's
  *      marching_cubes, replaced by a table derived in this project) ------- */
 
@@ -189,9 +195,10 @@ int mpl_mc_emit(const float* S_dev, int64_t N, float iso, float voxel_size,
  * loads the library until exit), so N is limited to 256; a larger N returns
  * MPL_ERR_CAPACITY.  The first call on each device does one-time set-up
  * (it looks up the array's device address and uploads the case tables);
- * make that first call before any stream capture.  Calls that overlap on
- * the GPU share the
- * array and race: order them on one stream.  Output as mpl_mc_emit, with
+ * make that first call before any stream capture.  First calls from several
+ * host threads at once are safe: the set-up is serialised and done once.
+ * Calls that overlap on the GPU share the array and race: order them on one
+ * stream.  Output as mpl_mc_emit, with
  * counts_dev[0], [1] = the full vertex and triangle counts (int64); output
  * beyond max_verts / max_tris is dropped, so counts above the capacities
  * mean the mesh was cut short. */
@@ -355,7 +362,10 @@ int mpl_adam_step(int32_t count, float* const* params_dev, const float* const* g
  * overlap them.  Setup, not the hot path: mpl_scene_create synchronises
  * `stream` and allocates the scene's device memory itself (the one exception
  * to the caller-owned-memory rule; mpl_scene_destroy waits for the device's
- * queued work and frees it).  positions
+ * queued work and frees it).  mpl_scene_destroy synchronises the whole
+ * device (cudaDeviceSynchronize: every stream of the process is waited for),
+ * so it must not run while any thread is capturing a CUDA graph, whose
+ * capture that synchronisation would invalidate.  positions
  * [n_positions, 3] float32, faces [n_faces, 3] int32; a face index outside
  * [0, n_positions) gives MPL_ERR_INVALID_ARG.  The scene copies the corners:
  * the inputs may be freed after the call.  Queries must be made with the
@@ -375,17 +385,19 @@ int mpl_scene_compute_distance(const MplScene* scene, const float* points_dev, i
                                float* distances_dev, void* stream);
 /* calc_deltas (experiment_scripts/utils.py:46-89): out [n_vertices, cols + 1]
  * is the input rows (cols >= 6: xyz, normal, ...) with the normal
- * normalised and the bisected neighbourhood radius appended.  step0 =
- * max_delta / n_iters in float32; the loop runs while max(delta) <
- * max_delta, n_iters times at most (the reference uses eps 2e-4).  scratch
+ * normalised and the bisected neighbourhood radius appended.  step0 is the
+ * first step, max_delta / n_iters as the reference computes it (utils.py:57:
+ * in double for a Python float max_delta, in float32 for a float32 tensor,
+ * then rounded to float32); the loop runs while max(delta) < max_delta,
+ * n_iters times at most (the reference uses eps 2e-4).  scratch
  * is sized by mpl_calc_deltas_scratch_bytes (256-byte aligned).
  * iterations_dev (nullable, device int32) receives the number of
  * iterations run.  Results equal the reference loop over an exact
  * nearest-triangle distance bit for bit. */
 int mpl_calc_deltas_scratch_bytes(int64_t n_vertices, int32_t n_iters, int64_t* bytes);
 int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev, int64_t n_vertices,
-                    int32_t cols, float max_delta, int32_t n_iters, float eps, void* scratch_dev,
-                    float* out_dev, int32_t* iterations_dev, void* stream);
+                    int32_t cols, float max_delta, float step0, int32_t n_iters, float eps,
+                    void* scratch_dev, float* out_dev, int32_t* iterations_dev, void* stream);
 
 /* ---- batched evaluation of many levels of many models ------------------- */
 /* No single reference entry point: this replaces the reference's one launch
@@ -471,6 +483,15 @@ const char* mpl_status_string(int status);
  * bounded device-side waits set when they give up (MPL_ERR_DEVICE_TIMEOUT);
  * *status_out is MPL_OK when no wait gave up. */
 int mpl_device_status(int32_t* status_out);
+/* Exercises the bounded-wait contract.  No counterpart in the reference: its
+ * kernels have no device-side waits and it reports errors through CUDA's own
+ * status (CUDA_CHECK_THROW, renderer/cuda/tools.cu:9-37).  One CTA runs the kernels' wait routine on
+ * mbarriers that nothing arrives at: warp 0 with limit_ns (1 ms .. 2 s) must
+ * give up and record MPL_ERR_DEVICE_TIMEOUT, warp 1 with the kernels' own
+ * limit must leave through the abort flag warp 0 raised.  result_dev [4]
+ * int64: whether each warp's wait succeeded, and the nanoseconds each
+ * waited.  No copy or MMA is in flight, so the context stays usable. */
+int mpl_wait_selftest(int64_t limit_ns, int64_t* result_dev, void* stream);
 /* cudaError_t of the most recent failed CUDA call in this thread. */
 int mpl_last_cuda_error(void);
 int mpl_abi_version(void);

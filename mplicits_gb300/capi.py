@@ -124,6 +124,7 @@ SIGNATURES = {
                                           _I32, _P]),
     "mpl_grid_points": (ctypes.c_int, [ctypes.POINTER(MplPoints), _P, _I64, _P, _P]),
     "mpl_band_compact": (ctypes.c_int, [_P, _P, _P, _I64, ctypes.POINTER(MplBand), _P]),
+    "mpl_abs_max": (ctypes.c_int, [_P, _I64, _P, _P]),
     "mpl_mc_workspace_bytes": (ctypes.c_int, [_I64, ctypes.POINTER(_I64)]),
     "mpl_mc_count": (ctypes.c_int, [_P, _I64, _F, _P, _P, _P]),
     "mpl_mc_emit": (ctypes.c_int, [_P, _I64, _F, _F, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
@@ -154,7 +155,7 @@ SIGNATURES = {
                                       ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "mpl_scene_compute_distance": (ctypes.c_int, [_P, _P, _I64, _P, _P]),
     "mpl_calc_deltas_scratch_bytes": (ctypes.c_int, [_I64, _I32, ctypes.POINTER(_I64)]),
-    "mpl_calc_deltas": (ctypes.c_int, [_P, _P, _I64, _I32, _F, _I32, _F, _P, _P, _P, _P]),
+    "mpl_calc_deltas": (ctypes.c_int, [_P, _P, _I64, _I32, _F, _F, _I32, _F, _P, _P, _P, _P]),
     "mpl_batch_workspace_bytes": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
     "mpl_batch_prepare": (ctypes.c_int, [ctypes.POINTER(MplBatchEntry), _I32, _I32, _P, _I64,
                                          ctypes.POINTER(MplBatchPlan), _P]),
@@ -167,6 +168,7 @@ SIGNATURES = {
     "mpl_get_option": (ctypes.c_int, [_I32, ctypes.POINTER(_I64)]),
     "mpl_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "mpl_device_status": (ctypes.c_int, [ctypes.POINTER(_I32)]),
+    "mpl_wait_selftest": (ctypes.c_int, [_I64, _P, _P]),
     "mpl_last_cuda_error": (ctypes.c_int, []),
     "mpl_abi_version": (ctypes.c_int, []),
 }

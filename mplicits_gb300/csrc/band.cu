@@ -39,9 +39,38 @@ __global__ void band_compact_kernel(const float* __restrict__ S, const int32_t* 
   }
 }
 
+// max_j |S_j| as float bits: for non-negative floats the unsigned order of
+// the bits is the numeric order, and a NaN's bits (0x7fc00000 and up) lie
+// above +inf's, so one NaN makes the result NaN, as torch's max does.
+__global__ void abs_max_kernel(const float* __restrict__ S, int64_t n,
+                               unsigned int* __restrict__ out) {
+  unsigned int m = 0u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const unsigned int v = __float_as_uint(S[i]) & 0x7fffffffu;
+    m = v > m ? v : m;
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 }  // namespace mpl
 
 using namespace mpl;
+
+extern "C" int mpl_abs_max(const float* S, int64_t n, float* out, void* stream) {
+  if (!out || n < 0 || (n > 0 && !S)) return MPL_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  MPL_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float), s));
+  if (n == 0) return MPL_OK;
+  const int threads = 256;
+  int64_t blocks = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)sm_count() * 8;
+  if (blocks > cap) blocks = cap;
+  abs_max_kernel<<<(unsigned)blocks, threads, 0, s>>>(S, n, reinterpret_cast<unsigned int*>(out));
+  MPL_LAUNCH_CHECK();
+  return MPL_OK;
+}
 
 extern "C" int mpl_band_compact(const float* S, const int32_t* index, const int32_t* n_dev,
                                 int64_t n, const MplBand* band, void* stream) {

@@ -1,6 +1,8 @@
 // extern "C" entry points of libmplicits: argument validation and dispatch.
 #include <string.h>
 
+#include <atomic>
+
 #include "level.cuh"
 
 namespace mpl {
@@ -8,15 +10,18 @@ namespace mpl {
 __device__ int g_device_status = 0;
 
 int* device_status_ptr() {
-  static int* cached[64] = {nullptr};
+  // looked up once per device; concurrent first calls store the same address
+  static std::atomic<int*> cached[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!cached[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_device_status) != cudaSuccess) return nullptr;
-    cached[dev] = (int*)p;
+  int* p = cached[dev].load(std::memory_order_acquire);
+  if (!p) {
+    void* q = nullptr;
+    if (cudaGetSymbolAddress(&q, g_device_status) != cudaSuccess) return nullptr;
+    p = (int*)q;
+    cached[dev].store(p, std::memory_order_release);
   }
-  return cached[dev];
+  return p;
 }
 
 static thread_local int t_last_cuda_error = 0;

@@ -91,16 +91,18 @@ __device__ __forceinline__ float sin_fast(float z, float phase) { return __sinf(
 
 // Bounded wait: the thread sleeps in hardware between polls (up to 20 us a
 // poll), leaves early when another role raised the abort flag, and gives up
-// after kWaitLimitNs of wall time, recording MPL_ERR_DEVICE_TIMEOUT.
+// after limit_ns of wall time (kWaitLimitNs in the kernels; the wait
+// self-test passes a shorter one), recording MPL_ERR_DEVICE_TIMEOUT.
 __device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, int* status,
-                                                volatile int* abort_flag) {
+                                                volatile int* abort_flag,
+                                                uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_timer_ns();
   for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait_sleep(bar, parity, 20000u)) return true;
     if ((i & 7) == 0) {
       if (*abort_flag) return false;
-      if (global_timer_ns() - t0 > kWaitLimitNs) break;
+      if (global_timer_ns() - t0 > limit_ns) break;
     }
   }
   report_device_error(status, MPL_ERR_DEVICE_TIMEOUT);

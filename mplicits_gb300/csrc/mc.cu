@@ -13,6 +13,9 @@
 // Output order is canonical (see mplicits.h) and matches the CPU restatement
 // in oracle/mc.c bit for bit: all arithmetic is float32 with explicit
 // round-to-nearest intrinsics and no contraction.
+#include <atomic>
+#include <mutex>
+
 #include "common.cuh"
 #include "mc_tables.h"
 
@@ -410,17 +413,24 @@ __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(
   }
 }
 
-bool g_tables_loaded[64] = {false};
+// Per-device one-time set-up (case tables here, the no-allocation
+// workspace's address below): the flags are read without a lock on the fast
+// path; the first calls on a device, from any number of host threads,
+// serialise on g_setup_mutex, so the upload happens once.
+std::atomic<bool> g_tables_loaded[64];
+std::mutex g_setup_mutex;
 
 int ensure_tables() {
   int dev = 0;
   MPL_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return MPL_ERR_INVALID_ARG;
-  if (g_tables_loaded[dev]) return MPL_OK;
+  if (g_tables_loaded[dev].load(std::memory_order_acquire)) return MPL_OK;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (g_tables_loaded[dev].load(std::memory_order_relaxed)) return MPL_OK;
   MPL_CUDA_TRY(cudaMemcpyToSymbol(c_tri_count, MPL_MC_TRI_COUNT, sizeof(MPL_MC_TRI_COUNT)));
   MPL_CUDA_TRY(cudaMemcpyToSymbol(c_tri_edges, MPL_MC_TRI_EDGES, sizeof(MPL_MC_TRI_EDGES)));
   MPL_CUDA_TRY(cudaMemcpyToSymbol(c_edge, MPL_MC_EDGE, sizeof(MPL_MC_EDGE)));
-  g_tables_loaded[dev] = true;
+  g_tables_loaded[dev].store(true, std::memory_order_release);
   return MPL_OK;
 }
 
@@ -508,16 +518,20 @@ __device__ __align__(256) unsigned char g_mc_static_ws[static_ws_bytes(kStaticMa
 // symbol itself is only a host-side stand-in, so the address is looked up
 // once per device (with that device current) and cached.
 int static_ws_address(void** out) {
-  static void* cached[64] = {nullptr};
+  static std::atomic<void*> cached[64];
   int dev = 0;
   MPL_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return MPL_ERR_INVALID_ARG;
-  if (!cached[dev]) {
-    void* p = nullptr;
-    MPL_CUDA_TRY(cudaGetSymbolAddress(&p, g_mc_static_ws));
-    cached[dev] = p;
+  void* p = cached[dev].load(std::memory_order_acquire);
+  if (!p) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    p = cached[dev].load(std::memory_order_relaxed);
+    if (!p) {
+      MPL_CUDA_TRY(cudaGetSymbolAddress(&p, g_mc_static_ws));
+      cached[dev].store(p, std::memory_order_release);
+    }
   }
-  *out = cached[dev];
+  *out = p;
   return MPL_OK;
 }
 

@@ -817,11 +817,11 @@ extern "C" int mpl_calc_deltas_scratch_bytes(int64_t n_vertices, int32_t n_iters
 }
 
 extern "C" int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev,
-                               int64_t n_vertices, int32_t cols, float max_delta,
+                               int64_t n_vertices, int32_t cols, float max_delta, float step0,
                                int32_t n_iters, float eps, void* scratch_dev, float* out_dev,
                                int32_t* iterations_dev, void* stream) {
   if (!scene || !vertices_dev || !out_dev || !scratch_dev || n_vertices < 1 || cols < 6 ||
-      n_iters < 1 || !isfinite(max_delta) || !(eps >= 0.f))
+      n_iters < 1 || !isfinite(max_delta) || !isfinite(step0) || !(eps >= 0.f))
     return MPL_ERR_INVALID_ARG;
   if (((uintptr_t)scratch_dev & 255) != 0) return MPL_ERR_INVALID_ARG;
   const int dst = check_device(scene);
@@ -830,7 +830,6 @@ extern "C" int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev,
   float* maxd = (float*)scratch_dev;
   float* step = (float*)((char*)scratch_dev + ((n_iters + 1 + 63) / 64) * 256);
   MPL_CUDA_TRY(cudaMemsetAsync(maxd, 0, sizeof(float) * (n_iters + 1), s));
-  const float step0 = max_delta / (float)n_iters;  // IEEE division on the host
   deltas_init<<<blocks(n_vertices), kThreads, 0, s>>>(vertices_dev, n_vertices, cols, step0,
                                                       out_dev, step, maxd);
   MPL_LAUNCH_CHECK();

@@ -272,8 +272,12 @@ def save_ply(verts, faces, filename, vertex_attributes=None):
     ft = np.zeros(faces.shape[0], dtype=[("n", "u1"), ("v", "<i4", (3,))])
     ft["n"] = 3
     ft["v"] = faces
-    props = "\n".join(f"property {'float' if t.endswith('f4') else 'double'} {n}"
-                      for n, t in dtypes)
+    ply_types = {"f4": "float", "f8": "double", "u1": "uchar", "i1": "char", "u2": "ushort",
+                 "i2": "short", "u4": "uint", "i4": "int"}
+    for n, t in dtypes:
+        if t[1:] not in ply_types:
+            raise ValueError(f"vertex attribute {n!r}: PLY has no type for numpy dtype {t!r}")
+    props = "\n".join(f"property {ply_types[t[1:]]} {n}" for n, t in dtypes)
     header = (f"ply\nformat binary_little_endian 1.0\nelement vertex {verts.shape[0]}\n"
               f"{props}\nelement face {faces.shape[0]}\n"
               "property list uchar int vertex_indices\nend_header\n")

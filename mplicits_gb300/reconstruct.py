@@ -4,7 +4,7 @@
 Same positional arguments and flags, same printed lines and the same
 ``SAMPLING_TIME_S:<seconds>`` line that reproduce.py parses; the band-culled
 evaluation and marching cubes run on the GPU through libmplicits.  New flag:
-``--precision {fp32,bf16}`` (fp32, the plain form, is the default).
+``--precision {fp32,bf16,fp16}`` (fp32, the plain form, is the default).
 ``--input`` reads the training point cloud from a PLY file (ASCII or binary
 vertex x/y/z), which the reference reads with open3d.
 """
@@ -63,21 +63,42 @@ def read_ply_points(path):
 
 
 def adaptive_deltas(models, input_ply, device, eps=0.3, batch=2 ** 18):
-    """reconstruct.py:18-33: delta_i = (1 + eps) * max_j |sum_{k<i} f_k(x_j)|,
-    with the partial sums accumulated on the device by the level kernel."""
+    """reconstruct.py:18-33: delta_i = (1 + eps) * max_j |sum_{k<i} f_k(x_j)|.
+
+    ``input_ply`` is a PLY path or an [M, 3] point array.  The partial sums
+    are accumulated on the device by the level kernel (f0 stored, then each
+    f_k added, the float32 order of the reference's ``sum``), and each chunk's
+    ``max |S|`` is reduced on the device into its own slot (mpl_abs_max), so
+    the whole computation reads the host once.  The slots are then combined
+    as the reference's ``worst = max(worst, float(...))`` does, chunk by
+    chunk in order (a chunk whose maximum is NaN leaves ``worst`` unchanged).
+    """
     from .model import level_forward
-    pts = torch.from_numpy(read_ply_points(input_ply)).to(device)
-    deltas = []
+    src = read_ply_points(input_ply) if isinstance(input_ply, (str, os.PathLike)) else input_ply
+    pts = torch.as_tensor(np.asarray(src, np.float32)).to(device).contiguous()
+    M = pts.shape[0]
+    heads = list(range(0, M, batch))
+    lib = capi.load()
+    maxima = torch.zeros(max(len(models) - 1, 1), max(len(heads), 1), dtype=torch.float32,
+                         device=device)
+    S = torch.empty(min(batch, max(M, 1)), dtype=torch.float32, device=device)
     with torch.no_grad():
         for level in range(1, len(models)):
-            worst = 0.0
-            for i in range(0, pts.shape[0], batch):
+            for c, i in enumerate(heads):
                 chunk = pts[i:i + batch]
-                S = level_forward(models[0], chunk)
+                s = S[:chunk.shape[0]]
+                level_forward(models[0], chunk, S=s)
                 for k in range(1, level):
-                    level_forward(models[k], chunk, S=S, accumulate=True)
-                worst = max(worst, float(S.abs().max()))
-            deltas.append((1.0 + eps) * worst)
+                    level_forward(models[k], chunk, S=s, accumulate=True)
+                capi.check(lib.mpl_abs_max(capi.ptr(s), s.shape[0], capi.ptr(maxima[level - 1, c:]),
+                                           capi.stream_ptr()), "mpl_abs_max")
+    host = maxima.cpu().tolist()
+    deltas = []
+    for level in range(1, len(models)):
+        worst = 0.0
+        for m in host[level - 1][:len(heads)]:
+            worst = max(worst, m)
+        deltas.append((1.0 + eps) * worst)
     return deltas
 
 
@@ -102,8 +123,9 @@ def main(argv=None):
                         help="Training point cloud (.ply) for the adaptive band widths.")
     parser.add_argument("--deltas", type=float, nargs="+", default=None,
                         help="Explicit band widths (one per residual level).")
-    parser.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",
-                        help="Arithmetic of the hidden layers (fp32 plain form, or bf16 tcgen05).")
+    parser.add_argument("--precision", choices=["fp32", "bf16", "fp16"], default="fp32",
+                        help="Arithmetic of the hidden layers: fp32 (plain form), or bf16 / "
+                             "fp16 operands on the tcgen05 tensor cores.")
     args = parser.parse_args(argv)
     out_dir = osp.split(args.output_path)[0]
     if out_dir and not osp.exists(out_dir):

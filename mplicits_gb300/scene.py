@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
 import torch
 
 from . import capi
@@ -26,6 +27,12 @@ class RaycastingScene:
     takes positions [V, 3] and integer faces [F, 3] (tensors or arrays);
     a second call replaces the mesh.  ``cell`` is the grid's cell side
     (default: twice the mean edge length).
+
+    Building and releasing a scene synchronise: a replaced or collected
+    scene's memory is freed after a device-wide synchronisation.  Keep a
+    scene alive (and call no ``add_triangles``) while any stream of the
+    process is capturing a CUDA graph; that synchronisation would end the
+    capture with an error.
     """
 
     def __init__(self, positions=None, faces=None, device="cuda", cell=0.0):
@@ -89,18 +96,31 @@ class RaycastingScene:
             pass
 
 
+def first_step(max_delta, n_iters):
+    """float32 first step of calc_deltas, ``max_delta / n_iters``
+    (experiment_scripts/utils.py:57): a tensor divides in its own dtype, a
+    Python number in double; the loop then holds it as float32."""
+    if isinstance(max_delta, torch.Tensor):
+        return float((max_delta.detach().cpu() / n_iters).to(torch.float32).item())
+    if isinstance(max_delta, (np.ndarray, np.generic)):
+        return float(np.float32(np.asarray(max_delta) / n_iters))
+    return float(np.float32(float(max_delta) / n_iters))
+
+
 def calc_deltas(vertices, scene, max_delta=0.05, n_iters=100, device=None, eps=2e-4,
                 return_iterations=False):
     """Drop-in for experiment_scripts/utils.py:46-89.
 
     ``vertices`` [M, C >= 6] (xyz, normal, ...); returns [M, C + 1] on the
     scene's device: the rows with unit normals and the neighbourhood radius
-    appended.  ``max_delta`` may be a float or a 0-d tensor (the reference's
-    callers pass ``max |f(v)|`` as a tensor); it is used in float32, and the
-    first step is max_delta / n_iters in float32 (a device tensor is read
-    on the host once).  With ``return_iterations`` also returns the number
-    of iterations run (one more host read).  The iterations themselves run
-    without host round trips.
+    appended.  ``max_delta`` may be a Python number or a 0-d tensor (the
+    reference's callers pass ``max |f(v)|`` as a tensor); the loop compares
+    against it in float32, and the first step is ``max_delta / n_iters``
+    taken in max_delta's own precision (double for a Python number, float32
+    for a float32 tensor) and rounded to float32, as utils.py:57 does (a
+    device tensor is read on the host once).  With ``return_iterations``
+    also returns the number of iterations run (one more host read).  The
+    iterations themselves run without host round trips.
     """
     dev = scene.device if device is None else torch.device(device)
     if dev.type != "cuda" or (dev.index if dev.index is not None else torch.cuda.current_device()) \
@@ -117,6 +137,7 @@ def calc_deltas(vertices, scene, max_delta=0.05, n_iters=100, device=None, eps=2
     if int(n_iters) < 1:
         raise ValueError("n_iters must be >= 1")
     md = float(torch.as_tensor(max_delta, dtype=torch.float32).item())
+    step0 = first_step(max_delta, int(n_iters))
     nbytes = ctypes.c_int64()
     lib = capi.load()
     capi.check(lib.mpl_calc_deltas_scratch_bytes(M, int(n_iters), ctypes.byref(nbytes)),
@@ -125,7 +146,7 @@ def calc_deltas(vertices, scene, max_delta=0.05, n_iters=100, device=None, eps=2
     out = torch.empty(M, C + 1, dtype=torch.float32, device=dev)
     iters = torch.zeros(1, dtype=torch.int32, device=dev)
     with torch.cuda.device(dev):
-        capi.check(lib.mpl_calc_deltas(scene.handle, capi.ptr(V), M, C, md, int(n_iters),
+        capi.check(lib.mpl_calc_deltas(scene.handle, capi.ptr(V), M, C, md, step0, int(n_iters),
                                        float(eps), capi.ptr(scratch), capi.ptr(out),
                                        capi.ptr(iters), capi.stream_ptr()), "mpl_calc_deltas")
     if return_iterations:

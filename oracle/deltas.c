@@ -393,6 +393,8 @@ static int decide_bvh(const Bvh* h, const float* q, float delta, float eps, cons
 
 /* Runs calc_deltas on M vertices of C >= 6 columns (xyz, normal, ...),
  * writing [M, C + 1] rows (normal normalised, delta appended) to out.
+ * step0 is the first step, max_delta / n_iters as utils.py:57 computes it in
+ * max_delta's own precision, rounded to float32 (the caller computes it).
  * cell <= 0: brute-force distances; cell > 0: a grid with that cell side
  * (fast == 1: decide_fast on it, else the minimum over the cells in range);
  * fast == 2: decide_bvh on a hierarchy (cell unused).
@@ -401,11 +403,11 @@ static int decide_bvh(const Bvh* h, const float* q, float delta, float eps, cons
  * decided).  Returns the number of iterations run, or -1 on an argument
  * error. */
 int mpl_oracle_calc_deltas(const float* verts, int64_t M, int C, const float* pos, int64_t nv,
-                           const int32_t* faces, int64_t T, float max_delta, int n_iters,
-                           float eps, float cell, int force_iters, int fast, float* out) {
+                           const int32_t* faces, int64_t T, float max_delta, float step0,
+                           int n_iters, float eps, float cell, int force_iters, int fast,
+                           float* out) {
   if (M <= 0 || C < 6 || n_iters < 1) return -1;
   const int64_t W = C + 1;
-  const float step0 = max_delta / (float)n_iters;
   float* step = (float*)malloc(sizeof(float) * (size_t)M);
   for (int64_t i = 0; i < M; ++i) {
     float* o = out + i * W;

@@ -42,7 +42,7 @@ def _load():
         lib.mpl_oracle_tri_dist.argtypes = [P, P, P, P]
         lib.mpl_oracle_tri_dist.restype = F
         lib.mpl_oracle_compute_distance.argtypes = [P, P, I64, P, I64, P]
-        lib.mpl_oracle_calc_deltas.argtypes = [P, I64, ctypes.c_int, P, I64, P, I64, F,
+        lib.mpl_oracle_calc_deltas.argtypes = [P, I64, ctypes.c_int, P, I64, P, I64, F, F,
                                                ctypes.c_int, F, F, ctypes.c_int, ctypes.c_int,
                                                P]
         lib.mpl_oracle_calc_deltas.restype = ctypes.c_int
@@ -79,6 +79,17 @@ def compute_distance(positions, faces, points):
     return out
 
 
+def first_step(max_delta, n_iters):
+    """``step_delta = max_delta / n_iters`` of experiment_scripts/utils.py:57,
+    as the float32 value the loop starts from: the quotient is taken in
+    max_delta's own precision (double for a Python number, float32 for a
+    float32 scalar or 0-d array, which is what the trainers pass as a
+    tensor) and then rounded to float32."""
+    q = np.asarray(max_delta) / n_iters if isinstance(max_delta, (np.ndarray, np.generic)) \
+        else float(max_delta) / n_iters
+    return float(np.float32(q))
+
+
 def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-4, cell=0.0,
                 force_iters=None, fast=False, bvh=False):
     """The reference's calc_deltas: returns ([M, C + 1] float32 rows, the
@@ -99,7 +110,8 @@ def calc_deltas(vertices, positions, faces, max_delta=0.05, n_iters=100, eps=2e-
     pos, fc = _mesh(positions, faces)
     out = np.empty((M, C + 1), np.float32)
     it = _load().mpl_oracle_calc_deltas(_ptr(V), M, C, _ptr(pos), pos.shape[0], _ptr(fc),
-                                        fc.shape[0], float(np.float32(max_delta)), int(n_iters),
+                                        fc.shape[0], float(np.float32(max_delta)),
+                                        first_step(max_delta, int(n_iters)), int(n_iters),
                                         float(np.float32(eps)), float(cell),
                                         -1 if force_iters is None else int(force_iters),
                                         2 if bvh else (1 if fast else 0), _ptr(out))

@@ -16,8 +16,10 @@ import numpy as np
 from . import siren
 
 
-def camera_rays(cam, radius=1.2):
-    """(origins, dirs, state) like mpl_trace_init (state 0 marching, 2 miss)."""
+def camera_rays(cam, radius=1.2, pixels=None):
+    """(origins, dirs, state) like mpl_trace_init (state 0 marching, 2 miss),
+    for every pixel (row-major, row 0 at the top) or for the pixel indices
+    ``pixels`` only (rays are independent)."""
     eye = np.asarray(cam["eye"], np.float64)
     tgt = np.asarray(cam["target"], np.float64)
     up = np.asarray(cam["up"], np.float64)
@@ -28,8 +30,9 @@ def camera_rays(cam, radius=1.2):
     s /= np.linalg.norm(s)
     u = np.cross(s, f)
     th = math.tan(0.5 * math.radians(cam["fov"]))
-    i = np.tile(np.arange(W), H)
-    j = np.repeat(np.arange(H), W)
+    r = np.arange(W * H) if pixels is None else np.asarray(pixels, np.int64)
+    i = r % W
+    j = r // W
     nx = 2.0 * i / W - 1.0
     ny = 1.0 - 2.0 * j / H
     d = (s[None] * (nx * th * W / H)[:, None] + u[None] * (ny * th)[:, None] + f[None])
@@ -61,10 +64,11 @@ def banded_sum(levels, deltas, x):
     return S, masks
 
 
-def trace(levels, deltas, cam, max_steps=96, eps=1e-4, radius=1.2):
+def trace(levels, deltas, cam, max_steps=96, eps=1e-4, radius=1.2, pixels=None):
     """Returns origins (final positions), state (1 hit, 2 miss, 3 budget)
-    and the summed level gradients at the hits."""
-    o, d, state = camera_rays(cam, radius)
+    and the summed level gradients at the hits, for every pixel or for the
+    pixel indices ``pixels``."""
+    o, d, state = camera_rays(cam, radius, pixels)
     for k in range(max_steps):
         act = np.nonzero(state == 0)[0]
         if act.size == 0:
@@ -91,3 +95,62 @@ def trace(levels, deltas, cam, max_steps=96, eps=1e-4, radius=1.2):
                 g[m] += siren.siren_input_grad(*levels[i], x[m])
         G[hits] = g
     return o, state, G
+
+
+def banded_gradient(levels, deltas, x):
+    """Sum of the level gradients at x with the finer levels gated by their
+    bands (the normals of kernels.cu:65-120 with band gating), float64;
+    also the partial sums S_0, S_0 + S_1, ... that decided the gating."""
+    S, masks = banded_sum(levels, deltas, x)
+    g = siren.siren_input_grad(*levels[0], x)
+    partial = [siren.siren_forward(*levels[0], x, np.float64)]
+    for i in range(1, len(levels)):
+        m = masks[i - 1]
+        if m.any():
+            g[m] += siren.siren_input_grad(*levels[i], x[m])
+        nxt = partial[-1].copy()
+        if m.any():
+            nxt[m] += siren.siren_forward(*levels[i], x[m], np.float64)
+        partial.append(nxt)
+    return g, S, partial
+
+
+def shade(org, dirs, G, state, mode=1):
+    """RGBA8 pixels (packed little-endian into uint32) of Shade_kernel,
+    renderer/cuda/kernels.cu:191-268, in float32: a hit inside the unit cube
+    gets, with n = G/|G| and the light along the view direction l = -d,
+    0.2 + 1 * max(n.l, 0) * 0.54 + 0.5 * max((l.r)^35, 0) on every channel,
+    r = 2 (n.l) n - l (mode 1), or (|n_x|, |n_z|, |n_y|) (mode 0); every
+    other pixel is white.  Channels are clamp(c, 0, 1) * 255 truncated
+    (kernels.cu:29-39)."""
+    f32 = np.float32
+    org = np.asarray(org, f32)
+    dirs = np.asarray(dirs, f32)
+    G = np.asarray(G, f32)
+    n = G.shape[0]
+
+    def q(v):
+        return (np.clip(v, f32(0), f32(1)) * f32(255)).astype(np.uint32)
+
+    def pack(r, g, b):
+        return (np.uint32(255) << np.uint32(24)) | (q(b) << np.uint32(16)) | \
+            (q(g) << np.uint32(8)) | q(r)
+
+    white = pack(np.ones(n, f32), np.ones(n, f32), np.ones(n, f32))
+    inside = (np.abs(org) < f32(1)).all(1)
+    hit = (np.asarray(state) == 1) & inside
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ln = np.sqrt((G * G).sum(1, dtype=f32)).astype(f32)
+        nrm = (G / ln[:, None]).astype(f32)
+        if mode == 0:
+            img = pack(np.abs(nrm[:, 0]), np.abs(nrm[:, 2]), np.abs(nrm[:, 1]))
+        else:
+            l = -dirs
+            nl = (l * nrm).sum(1, dtype=f32).astype(f32)
+            refl = (f32(2) * nl[:, None] * nrm - l).astype(f32)
+            rv = (l * refl).sum(1, dtype=f32).astype(f32)
+            spec = np.maximum(np.power(np.maximum(rv, f32(0)), f32(35)), f32(0)).astype(f32)
+            c = (f32(0.2) + f32(1) * np.maximum(nl, f32(0)) * f32(0.54) + f32(0.5) * spec)
+            c = c.astype(f32)
+            img = pack(c, c, c)
+    return np.where(hit, img, white).astype(np.uint32)

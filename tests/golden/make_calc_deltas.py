@@ -1,9 +1,9 @@
 """Golden vectors of the tubular-neighbourhood deltas (calc_deltas).
 
-    python tests/golden/make_calc_deltas.py
+    python tests/golden/make_calc_deltas.py --ref <reference checkout>
 
 Runs the reference's own ``calc_deltas`` (experiment_scripts/utils.py:46-89)
-from the read-only reference tree at ``/root/reference``.  Its scene is an
+from a reference checkout (``--ref`` or ``MPLICITS_REFERENCE``).  Its scene is an
 open3d ``RaycastingScene`` (open3d 0.19.0, not installed); here a stand-in
 object answers ``compute_distance`` with the oracle's float32 point-triangle
 distance (oracle/deltas.c, brute force over all triangles) and counts its
@@ -26,7 +26,13 @@ import types
 import numpy as np
 import torch
 
-REF = "/root/reference"
+REF = None  # the reference checkout: main() sets it from --ref PATH or MPLICITS_REFERENCE
+
+
+def _reference_root():
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from refroot import reference_root
+    return reference_root()
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
@@ -113,10 +119,21 @@ def cases():
     # a vertex on no triangle, far away: its distance exceeds delta + eps
     Viso = np.concatenate([Vslab, np.array([[3.0, 3.0, 3.0, 0, 0, 1]], np.float32)])
     out.append(("isolated_vertex", Viso, sp, sf, 0.2, 60))
+    # max_delta as a Python float: the first step is a double quotient
+    # rounded to float32, one ulp away from the float32 quotient for these
+    out.append(("float_max_delta", V, pos, faces, 0.03, 100))
+    out.append(("float_max_delta_1000", V, pos, faces, 0.1, 1000))
     return out
 
 
+# cases whose max_delta is passed as a Python float (the rest as a 0-d
+# float32 tensor, as the reference's trainers do)
+FLOAT_CASES = {"float_max_delta", "float_max_delta_1000"}
+
+
 def main():
+    global REF
+    REF = _reference_root()
     _stub()
     from utils import calc_deltas  # the reference module
 
@@ -127,15 +144,17 @@ def main():
     names = []
     for name, V, pos, faces, max_delta, n_iters in cases():
         scene = Scene(pos, faces)
-        # the reference's callers pass max_delta as a 0-d float32 tensor
-        md = torch.tensor(max_delta, dtype=torch.float32)
+        # the reference's trainers pass max_delta as a 0-d float32 tensor
+        md = max_delta if name in FLOAT_CASES else torch.tensor(max_delta, dtype=torch.float32)
         res = calc_deltas(torch.from_numpy(V.copy()), scene, max_delta=md, n_iters=n_iters,
                           device=torch.device("cpu"))
         names.append(name)
         arrays[f"{name}__vertices"] = V
         arrays[f"{name}__positions"] = pos
         arrays[f"{name}__faces"] = faces
-        arrays[f"{name}__max_delta"] = np.float32(max_delta)
+        arrays[f"{name}__max_delta"] = np.float64(max_delta) if name in FLOAT_CASES \
+            else np.float32(max_delta)
+        arrays[f"{name}__max_delta_kind"] = np.array("float" if name in FLOAT_CASES else "tensor")
         arrays[f"{name}__n_iters"] = np.int32(n_iters)
         arrays[f"{name}__out"] = res.numpy().astype(np.float32)
         arrays[f"{name}__iterations"] = np.int32(scene.calls)

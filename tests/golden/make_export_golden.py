@@ -1,11 +1,11 @@
 """Golden output of the reference's renderer exporter.
 
-    python tests/golden/make_export_golden.py
+    python tests/golden/make_export_golden.py --ref <reference checkout>
 
 Writes the three levels of tests/golden/tiny_three_level.npz as
 results/tiny/{coarse,medium,fine}/best.pth in a temporary folder, runs the
-reference's own renderer/scripts/export_experiment.py on it (from the
-read-only reference tree at /root/reference), and stores the .bin pairs and
+reference's own renderer/scripts/export_experiment.py on it (from a
+reference checkout, ``--ref`` or ``MPLICITS_REFERENCE``), and stores the .bin pairs and
 the .exp descriptor it wrote under tests/golden/export_experiment/.  The
 descriptor's first line names the absolute results folder; the fixture keeps
 the relative name the script was given, so the line is reproducible.
@@ -22,11 +22,19 @@ import tempfile
 import numpy as np
 import torch
 
-REF = "/root/reference"
+REF = None  # the reference checkout: main() sets it from --ref PATH or MPLICITS_REFERENCE
+
+
+def _reference_root():
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from refroot import reference_root
+    return reference_root()
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
+    global REF
+    REF = _reference_root()
     d = np.load(os.path.join(HERE, "tiny_three_level.npz"))
     out_dir = os.path.join(HERE, "export_experiment")
     os.makedirs(out_dir, exist_ok=True)

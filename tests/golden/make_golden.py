@@ -1,9 +1,10 @@
 """Generate the golden vectors that pin the oracle to the reference.
 
-Run in a container that holds the reference tree (read-only) at
-``/root/reference``:
+Run where a reference checkout is at hand:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --ref <reference checkout>
+
+(or with ``MPLICITS_REFERENCE`` set to it).
 
 It imports the reference's own ``i3d`` package.  ``i3d.meshing`` imports
 ``plyfile`` and ``skimage`` at module level; neither is installed, so both are
@@ -24,7 +25,13 @@ import types
 import numpy as np
 import torch
 
-REF = "/root/reference"
+REF = None  # the reference checkout: main() sets it from --ref PATH or MPLICITS_REFERENCE
+
+
+def _reference_root():
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from refroot import reference_root
+    return reference_root()
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 captured = {}
@@ -61,6 +68,8 @@ def state_dict_np(model):
 
 
 def main():
+    global REF
+    REF = _reference_root()
     _install_stubs()
     from i3d.model import SIREN
     from i3d import meshing, diff_operators

@@ -1,10 +1,10 @@
 """Golden vectors of the residual trainers' batch construction.
 
-    python tests/golden/make_train_batch.py
+    python tests/golden/make_train_batch.py --ref <reference checkout>
 
 Runs the reference's own ``create_training_data_on_neighborhood``
-(experiment_scripts/utils.py:92-169) from the read-only reference tree at
-``/root/reference`` on a small seeded vertex array, with and without the
+(experiment_scripts/utils.py:92-169) from a reference checkout
+(``--ref`` or ``MPLICITS_REFERENCE``) on a small seeded vertex array, with and without the
 neighbourhood delta column and dithering.  ``open3d`` and ``plyfile`` are
 imported at module level there but not used by this function, so both are
 stubbed.  The random draws the function makes (``torch.randperm`` for the
@@ -22,7 +22,13 @@ import types
 import numpy as np
 import torch
 
-REF = "/root/reference"
+REF = None  # the reference checkout: main() sets it from --ref PATH or MPLICITS_REFERENCE
+
+
+def _reference_root():
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from refroot import reference_root
+    return reference_root()
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -44,6 +50,8 @@ def _stub():
 
 
 def main():
+    global REF
+    REF = _reference_root()
     _stub()
     from utils import create_training_data_on_neighborhood  # the reference module
 

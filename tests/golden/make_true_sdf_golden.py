@@ -2,10 +2,10 @@
 (i3d/loss_functions.py:123-163), and the parameter gradients autograd gives
 for it, from the reference's own code.
 
-    python tests/golden/make_true_sdf_golden.py
+    python tests/golden/make_true_sdf_golden.py --ref <reference checkout>
 
-Imports i3d.model and i3d.loss_functions from the read-only reference tree at
-/root/reference; writes tests/golden/loss_true_sdf.npz.
+Imports i3d.model and i3d.loss_functions from a reference checkout (``--ref``
+or ``MPLICITS_REFERENCE``); writes tests/golden/loss_true_sdf.npz.
 """
 
 from __future__ import annotations
@@ -16,11 +16,19 @@ import sys
 import numpy as np
 import torch
 
-REF = "/root/reference"
+REF = None  # the reference checkout: main() sets it from --ref PATH or MPLICITS_REFERENCE
+
+
+def _reference_root():
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from refroot import reference_root
+    return reference_root()
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
+    global REF
+    REF = _reference_root()
     sys.path.insert(0, REF)
     from i3d.loss_functions import true_sdf
     from i3d.model import SIREN

@@ -23,7 +23,10 @@ def _golden():
                                            (0.0, False, True)])
 def test_oracle_equals_reference_loop(cell, fast, bvh):
     for name, c in _golden():
-        out, it = od.calc_deltas(c["vertices"], c["positions"], c["faces"], c["max_delta"],
+        # a Python float, or the float32 value of the reference's tensor
+        md = float(c["max_delta"]) if str(c["max_delta_kind"]) == "float" \
+            else np.float32(c["max_delta"])
+        out, it = od.calc_deltas(c["vertices"], c["positions"], c["faces"], md,
                                  int(c["n_iters"]), cell=cell, fast=fast, bvh=bvh)
         assert it == int(c["iterations"]), name
         np.testing.assert_array_equal(out, c["out"], err_msg=name)

@@ -26,7 +26,8 @@ def test_golden_bit_exact(cell):
     from mplicits_gb300.scene import RaycastingScene, calc_deltas
     for name, c in _golden():
         scene = RaycastingScene(c["positions"], c["faces"], cell=cell)
-        md = torch.tensor(float(c["max_delta"]), dtype=torch.float32)
+        md = float(c["max_delta"]) if str(c["max_delta_kind"]) == "float" \
+            else torch.tensor(float(c["max_delta"]), dtype=torch.float32)
         out, it = calc_deltas(torch.from_numpy(c["vertices"]), scene, max_delta=md,
                               n_iters=int(c["n_iters"]), return_iterations=True)
         assert it == int(c["iterations"]), name

@@ -107,3 +107,28 @@ def test_refined_tensor_core_bands_and_mesh_topology_equal_fp32(lib, precision, 
     S32, S16 = ref.S.cpu().numpy(), rec.S.cpu().numpy()
     near = np.abs(S16) < margin  # the points the zero-level pass recomputed in FP32
     assert near.any() and np.array_equal(S32[near], S16[near])
+
+
+def test_create_mesh_single_level_drop_in(lib, tmp_path):
+    """create_mesh (i3d/meshing.py:72-132): one level on the whole grid, then
+    marching cubes.  The volume is within 1e-5 of the oracle's float32
+    evaluation, and the mesh is the oracle's marching cubes of the GPU
+    volume bit for bit; the PLY holds that mesh."""
+    from mplicits_gb300.meshing import BandedReconstruction, create_mesh
+    levels, sds, d = tiny_levels()
+    N = 40
+    path = os.path.join(tmp_path, "single.ply")
+    model = _models(sds)[0]
+    verts, faces, normals, values = create_mesh(model, filename=path, N=N, device="cuda",
+                                                silent=True)
+    rec = BandedReconstruction([model], [], N, "cuda")
+    S = rec.sample().cpu().numpy()
+    ref, _ = siren.multistage_sdf(levels[:1], [], N)
+    assert np.abs(S - ref).max() <= 1e-5
+    v2, f2, n2, val2 = mc.marching_cubes_raw(S.reshape(N, N, N), 0.0, np.float32(2.0 / (N - 1)),
+                                             (-1, -1, -1))
+    assert verts.shape[0] > 100
+    for a, b in ((verts, v2), (faces, f2), (normals, n2), (values, val2)):
+        assert np.array_equal(a, b)
+    head = open(path, "rb").read().split(b"end_header\n")[0].decode()
+    assert f"element vertex {verts.shape[0]}" in head and f"element face {faces.shape[0]}" in head

@@ -39,3 +39,33 @@ def test_save_ply_vertex_attributes(tmp_path):
                            "property float nx", "property float ny", "property float nz"]
     v = np.frombuffer(body[:3 * 24], "<f4").reshape(3, 6)
     assert np.array_equal(v, verts)
+
+
+def test_save_ply_integer_and_double_attributes(tmp_path):
+    """Each attribute's header type matches the bytes written for it, so a
+    PLY reader recovers the values (uchar colour, int label, double weight)."""
+    from mplicits_gb300.meshing import save_ply
+    from mplicits_gb300.reconstruct import read_ply_points
+    verts = np.array([[0.5, 0, 0, 200, -7, 0.25], [1, 0.25, 0, 3, 9, 1e-9],
+                      [0, 1, -0.75, 255, 0, -2.5]], np.float64)
+    faces = np.array([[0, 1, 2]])
+    p = tmp_path / "a.ply"
+    attrs = [("red", "u1"), ("label", "i4"), ("weight", "f8")]
+    save_ply(verts, faces, str(p), vertex_attributes=attrs)
+    header, body = _read(p)
+    assert header[6:9] == ["property uchar red", "property int label", "property double weight"]
+    dt = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("red", "u1"), ("label", "<i4"),
+                   ("weight", "<f8")])
+    v = np.frombuffer(body[:3 * dt.itemsize], dtype=dt)
+    assert np.array_equal(v["red"], [200, 3, 255])
+    assert np.array_equal(v["label"], [-7, 9, 0])
+    assert np.array_equal(v["weight"], verts[:, 5])
+    assert np.array_equal(read_ply_points(str(p)), verts[:, :3].astype(np.float32))
+
+
+def test_save_ply_rejects_types_ply_cannot_name(tmp_path):
+    import pytest
+    from mplicits_gb300.meshing import save_ply
+    with pytest.raises(ValueError):
+        save_ply(np.zeros((3, 4)), np.array([[0, 1, 2]]), str(tmp_path / "b.ply"),
+                 vertex_attributes=[("t", "i8")])
