@@ -28,10 +28,6 @@ import subprocess
 import sys
 import time
 
-if "reference" in sys.argv:  # the CPU arm parallelises over chunks itself
-    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ.setdefault(var, "1")
-
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -56,7 +52,8 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--N", type=int, default=512)
     ap.add_argument("--fp32-steps", type=int, default=2)
-    ap.add_argument("--cpu-slabs", type=int, default=16, help="grid slabs timed on the CPU")
+    ap.add_argument("--cpu-repeats", type=int, default=3,
+                    help="CPU samples of the GPU line's cpu_baseline leg")
     ap.add_argument("--skip-errors", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--bf16-unit", type=int, default=None, choices=[16, 32],
@@ -88,13 +85,18 @@ def rank_info():
     return _ri()
 
 
-def peaks():
+def peaks(sustained=False):
+    """(bf16 TFLOP/s, HBM GB/s, source).  The burst bf16 figure is the
+    comparator of a kernel that runs at full clock with no power cap (the
+    level-0 launch of a 40 ms step); the sustained one is for kernels timed
+    inside long power-capped loops."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as f:
             p = json.load(f)
-        return p.get("bf16_tflops_sustained") or p["bf16_tflops"], p["hbm_gbs"], "measured"
-    return 1700.0, 6800.0, "fallback"
+        tf = (p.get("bf16_tflops_sustained") if sustained else None) or p["bf16_tflops"]
+        return tf, p["hbm_gbs"], "measured"
+    return (1700.0 if sustained else 1900.0), 6800.0, "fallback"
 
 
 class ClockSampler:
@@ -344,34 +346,40 @@ def e2e_run(levels_np, N, device, K, W):
     return dt, h2d, d2h[0], launches
 
 
-def cpu_baseline(levels_np, N, slabs, threads, gpu_S=None):
-    """The oracle port on the host cores: the band-culled evaluation of
-    ``slabs`` evenly spaced i-slabs of the grid (chunks over a thread pool),
-    extrapolated to the full grid, plus the oracle marching cubes (OpenMP) of
-    the full volume.  Returns (pts/s, detail)."""
-    from oracle import siren
-    levels = [(p, [30.0, 30.0, 30.0]) for _, p in levels_np]
-    sl = np.unique(np.linspace(0, N - 1, slabs).round().astype(np.int64))
-    index = (sl[:, None] * N * N + np.arange(N * N)[None, :]).reshape(-1)
+CPU_PAIRS = 4  # plane pairs per CPU sample step (2 * 4 * 512^2 = 2,097,152 points at 512^3)
+
+
+def config_of(N, world):
+    """The workload's description, the same in both arms' JSON lines."""
+    return {"workload": f"3-level band-culled reconstruction, {N}^3 grid ({N ** 3} points), "
+                        "3->256x3->1 SIREN levels (omega0 30, trained on the synthetic sphere), "
+                        "deltas 0.05/0.01, marching cubes",
+            "grid": N, "deltas": DELTAS,
+            "l2": f"working set larger than L2 (129 MB) at 512^3: the {4 * N ** 3 / 1e6:.0f} MB "
+                  "SDF volume is written and read every step",
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_reference_samples(N, repeats, pairs=CPU_PAIRS, threads=None):
+    """The reference's reconstruction loop on the host cores (oracle/
+    cpu_reference.py: its chunked torch sampling plus the C marching cubes),
+    ``repeats`` timed samples of ``pairs`` plane pairs each, run in a child
+    process whose thread environment is fixed here, so every CPU leg of the
+    benchmark measures the same thing.  Returns (pts/s per sample, detail,
+    wall seconds per sample)."""
+    threads = threads or os.cpu_count() or 1
+    env = dict(os.environ)
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        env[var] = str(threads)
+    env.pop("CUDA_VISIBLE_DEVICES", None)
+    cmd = [sys.executable, "-m", "oracle.cpu_reference", "--weights", WEIGHTS, "--N", str(N),
+           "--pairs", str(pairs), "--repeats", str(repeats), "--threads", str(threads),
+           "--deltas", *map(str, DELTAS)]
     t0 = time.perf_counter()
-    S, bands = siren.multistage_sdf_threaded(levels, DELTAS, N, index, threads)
-    t_sdf = time.perf_counter() - t0
-    t_mc = None
-    if gpu_S is not None:
-        from oracle import mc
-        vol = gpu_S.reshape(N, N, N)
-        t1 = time.perf_counter()
-        mc.marching_cubes_raw(vol, 0.0, np.float32(2.0 / (N - 1)), (-1, -1, -1))
-        t_mc = time.perf_counter() - t1
-    full = t_sdf * (N ** 3) / index.shape[0] + (t_mc or 0.0)
-    detail = {"sample": f"{len(sl)} evenly spaced {N}x{N} slabs of the {N}^3 grid "
-                        f"({index.shape[0]} points, bands {bands.tolist()}) timed, "
-                        "extrapolated to the full grid"
-                        + (", plus oracle marching cubes of the full volume" if t_mc else ""),
-              "sdf_seconds_sample": round(t_sdf, 3),
-              "mc_seconds_full": None if t_mc is None else round(t_mc, 3),
-              "seconds_full_estimate": round(full, 2)}
-    return N ** 3 / full, detail
+    out = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, check=True)
+    wall = (time.perf_counter() - t0) / max(1, repeats)
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    return res["values"], res["detail"], wall
 
 
 TRAIN_SURFACE = 1 << 16  # surface samples per batch; rows = 3x (surface, offset, dithered)
@@ -677,7 +685,7 @@ def batch_bench(device, K, W):
             "value": pts / (ms_batch * 1e-3), "unit": "pts/s", "ms_per_step": ms_batch,
             "achieved_tflops": flop / (ms_batch * 1e-3) / 1e12,
             "frac_of_peak": flop / (ms_batch * 1e-3) / 1e12 / peak_tf,
-            "peak_source": f"{src} bf16 sustained",
+            "peak_source": f"{src} bf16 burst",
             "autotuned": {"epilogue_unit": cfg.epilogue_unit, "stages": cfg.stages,
                           "ctas": cfg.ctas, "best_ms": tuned_ms, "tuning_s": round(tune_s, 3)},
             "per_level_bf16_ms": ms_bf16, "per_level_fp32_ms": ms_fp32,
@@ -687,28 +695,24 @@ def batch_bench(device, K, W):
 
 
 def run_reference(args):
+    """The reference arm: the reference's reconstruction loop on the host
+    cores (the oracle restatement of its torch code, which cannot travel),
+    W untimed and K timed samples of the same size as the GPU line's
+    cpu_baseline samples; rank 0 alone works and prints."""
     rank, world, _ = rank_info()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    levels_np = load_levels_np()
     K, W = max(1, args.steps), max(0, args.warmup)
-    slabs = max(2, args.cpu_slabs // 4)
-    for _ in range(min(W, 1)):
-        cpu_baseline(levels_np, args.N, 2, threads)
-    vals = []
-    for _ in range(K):
-        v, detail = cpu_baseline(levels_np, args.N, slabs, threads)
-        vals.append(v)
-    value = float(np.mean(vals))
+    vals, detail, wall = cpu_reference_samples(args.N, K + W)
+    timed = vals[W:]
+    value = float(np.mean(timed))
+    threads = detail["threads"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pts/s",
-            "n_gpus": world, "steps": K, "warmup": W, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"3-level band-culled reconstruction, {args.N}^3 grid, "
-                                   "3->256x3->1 SIREN levels, deltas 0.05/0.01 (CPU sample)",
-                       "grid": args.N, "deltas": DELTAS},
+            "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": wall * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(args.N, world),
             "cpu_baseline": {"value": value, "unit": "pts/s", "cores": threads, "kind": "port",
-                             "sample": detail["sample"]},
+                             "sample": f"mean of {len(timed)} samples: " + detail["sample"]},
             "e2e": {"value": value, "unit": "pts/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -838,25 +842,18 @@ def main():
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        v, detail = cpu_baseline(levels_np, N, args.cpu_slabs, os.cpu_count() or 1,
-                                 bf16.rec.S.cpu().numpy())
-        cpu = {"value": v, "unit": "pts/s", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": detail["sample"], "detail": detail}
+        vals, detail, _ = cpu_reference_samples(N, args.cpu_repeats)
+        cpu = {"value": float(np.mean(vals)), "unit": "pts/s", "cores": detail["threads"],
+               "kind": "port", "sample": f"mean of {len(vals)} samples: " + detail["sample"],
+               "samples": vals, "detail": detail}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "pts/s", "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": f"3-level band-culled reconstruction, {N}^3 grid "
-                                   f"({N ** 3} points), 3->256x3->1 SIREN levels (omega0 30, "
-                                   "trained on the synthetic sphere), deltas 0.05/0.01, "
-                                   "marching cubes on the device",
-                       "grid": N, "deltas": DELTAS, "band_points": bands,
-                       "mesh": {"verts": bf16.V, "faces": bf16.F},
-                       "l2": "working set larger than L2: the 537 MB SDF volume is written "
-                             "and read every step",
-                       "parallelism": f"replicas x{world}"},
+            "config": config_of(N, world),
+            "workload_stats": {"band_points": bands, "mesh": {"verts": bf16.V, "faces": bf16.F}},
             "banded_mc_ms": {"bf16_fused": ms, "fp32_plain": ms32},
             "variants": variants,
             "fp32_plain": {"value": N ** 3 / (ms32 * 1e-3), "unit": "pts/s", "ms_per_step": ms32,
@@ -869,7 +866,8 @@ def main():
                             "weights copied from pinned host memory and the mesh copied back"},
             "roofline": {"bound": "tensor", "kernel": kernel_name + " (level 0, full grid)",
                          "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-                         "frac": achieved_tf / peak_tf, "peak_source": f"{src} bf16 sustained",
+                         "frac": achieved_tf / peak_tf,
+                         "peak_source": f"{src} bf16 burst (the launch runs at full clock)",
                          "flop_per_point": FLOP_PER_POINT, "points_per_launch": N ** 3,
                          "launch_ms": l0_ms, "traffic": traffic},
             "cpu_baseline": cpu,

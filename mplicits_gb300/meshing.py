@@ -101,20 +101,35 @@ class BandedReconstruction:
     list is cut, and points with |S| < m after the last level get every level
     in FP32, so the band decisions and the marching-cubes signs are those of
     the plain FP32 path.
+
+    Band widths that never grow from one level to the next (the usual case)
+    make each band a subset of the previous one, so every level cuts the next
+    level's list as it stores (fused band lists).  When a width grows, the
+    reference's masks differ: level i runs on every point of a chunk of
+    ``chunk`` consecutive grid points with ``|S| < delta_{i-1}``, and a chunk
+    none of whose points was in band i stops there (i3d/meshing.py:221-231,
+    ``chunk`` is its ``max_batch``).  Those bands are cut by a compaction over
+    the whole grid and filtered by chunk on the device (one host read of each
+    band's size).
     """
 
-    def __init__(self, levels, deltas, N, device="cuda", precision=None, refine_margin=None):
+    def __init__(self, levels, deltas, N, device="cuda", precision=None, refine_margin=None,
+                 chunk=64 ** 3):
         self.levels = list(levels)
         self.deltas = list(deltas or [])
         self.N = int(N)
         self.device = torch.device(device)
         self.precision = precision
+        self.chunk = int(chunk)
+        if self.chunk < 1:
+            raise ValueError("chunk (max_batch) must be positive")
         if self.deltas and len(self.deltas) < len(self.levels) - 1:
             raise IndexError("deltas needs one entry per residual level")
-        if self.deltas and any(self.deltas[i + 1] > self.deltas[i]
-                               for i in range(len(self.levels) - 2)):
+        self.nested = not self.deltas or all(self.deltas[i + 1] <= self.deltas[i]
+                                             for i in range(len(self.levels) - 2))
+        if not self.nested and refine_margin:
             raise NotImplementedError(
-                "increasing band widths are not supported by the fused band lists")
+                "FP32 refinement margins need band widths that do not grow")
         n = self.N ** 3
         self.n = n
         self.voxel_size = 2.0 / (self.N - 1)
@@ -199,10 +214,43 @@ class BandedReconstruction:
         self._keep = keep
         return self.S
 
+    def _sample_general(self, stream):
+        """Bands of growing widths: level i on the points of the still-open
+        chunks with |S| < delta_{i-1}; a chunk with none closes."""
+        n, chunk = self.n, self.chunk
+        nchunks = (n + chunk - 1) // chunk
+        st = capi.stream_ptr(stream)
+        with torch.cuda.stream(stream) if stream is not None else torch.cuda.device(self.device):
+            self._level(0, self._prec(self.levels[0]), capi.MPL_STORE, st=st)
+            open_ = torch.ones(nchunks, dtype=torch.bool, device=self.device)
+            keep = []
+            for i in range(1, len(self.levels)):
+                lst, cnt = self.band_index[i - 1], self.band_count[i - 1:]
+                b = self._band(self.deltas[i - 1], lst, cnt)
+                keep.append(b)
+                self._compact(b, None, None, st)
+                m = int(cnt[0])  # host read: the band's size
+                idx = lst[:m].long()
+                ch = idx // chunk
+                sel = open_[ch]
+                idx, ch = idx[sel], ch[sel]
+                hit = torch.zeros(nchunks, dtype=torch.bool, device=self.device)
+                hit[ch] = True
+                open_ &= hit
+                lst[:idx.numel()] = idx.to(torch.int32)
+                cnt[0] = idx.numel()
+                self._level(i, self._prec(self.levels[i]), capi.MPL_ACCUMULATE, lst, cnt, None,
+                            st)
+            self._keep = keep
+        return self.S
+
     def sample(self, stream=None):
-        """Evaluate S over the grid (stream-ordered, no host sync)."""
+        """Evaluate S over the grid (stream-ordered; with nested band widths
+        no host sync)."""
         lib = capi.load()
         st = capi.stream_ptr(stream)
+        if not self.nested:
+            return self._sample_general(stream)
         if self.refine_margin and any(self._prec(mo) != capi.MPL_FP32 for mo in self.levels):
             return self._sample_refined(st)
         for i, model in enumerate(self.levels):
@@ -290,9 +338,11 @@ def save_ply(verts, faces, filename, vertex_attributes=None):
 def create_mesh_multistage(decoders, deltas=[], filename="", t=None, N=256, max_batch=64 ** 3,
                            offset=None, scale=None, device="cpu", silent=False, precision=None):
     """Drop-in for i3d/meshing.py:135-264; returns (verts, faces, normals,
-    values, sampling_time).  ``max_batch`` is accepted for compatibility: each
-    level runs as one launch over its whole point list.  ``precision``
-    ("fp32"/"bf16") overrides the decoders' own setting."""
+    values, sampling_time).  Each level runs as one launch over its whole
+    point list; ``max_batch`` matters only when a band width grows from one
+    level to the next, where the reference's per-chunk masks depend on it.
+    ``precision`` ("fp32", "bf16" or "fp16") overrides the decoders' own
+    setting."""
     if t is not None and t != -1:
         raise NotImplementedError("space-time (4-D) decoders are not part of the GB300 path")
     dev = torch.device(device)
@@ -300,7 +350,7 @@ def create_mesh_multistage(decoders, deltas=[], filename="", t=None, N=256, max_
         raise RuntimeError("mplicits_gb300 reconstructs on a CUDA device only (no CPU fallback)")
     for d in decoders:
         d.eval()
-    rec = BandedReconstruction(decoders, deltas, N, dev, precision)
+    rec = BandedReconstruction(decoders, deltas, N, dev, precision, chunk=max_batch)
     for d in decoders:  # pack outside the timing window, as the reference's weights
         d.packed()       # are already resident when its loop starts
     torch.cuda.synchronize(dev)

@@ -26,17 +26,20 @@
 
 static inline int inside(float v, float iso) { return v < iso; }
 
+/* A volume is NI x N x N (C order): NI = N for the cubes of
+ * i3d/meshing.py, NI < N for a slab of consecutive i-planes (the CPU
+ * baseline times slabs of the grid). */
 static inline int64_t lin(int64_t N, int64_t i, int64_t j, int64_t k) {
   return (i * N + j) * N + k;
 }
 
 /* Number of crossing edges owned by point (i,j,k) and its bit mask. */
-static inline int point_edges(const float* S, int64_t N, int64_t i, int64_t j, int64_t k,
-                              float iso) {
+static inline int point_edges(const float* S, int64_t NI, int64_t N, int64_t i, int64_t j,
+                              int64_t k, float iso) {
   int64_t p = lin(N, i, j, k);
   int s = inside(S[p], iso);
   int mask = 0;
-  if (i + 1 < N && inside(S[p + N * N], iso) != s) mask |= 1;
+  if (i + 1 < NI && inside(S[p + N * N], iso) != s) mask |= 1;
   if (j + 1 < N && inside(S[p + N], iso) != s) mask |= 2;
   if (k + 1 < N && inside(S[p + 1], iso) != s) mask |= 4;
   return mask;
@@ -53,15 +56,15 @@ static inline int cell_case(const float* S, int64_t N, int64_t i, int64_t j, int
 }
 
 /* Per-slab (fixed i) vertex and triangle counts. */
-void mpl_oracle_mc_count(const float* S, int64_t N, float iso, int64_t* slab_verts,
+void mpl_oracle_mc_count(const float* S, int64_t NI, int64_t N, float iso, int64_t* slab_verts,
                          int64_t* slab_tris) {
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t i = 0; i < N; ++i) {
+  for (int64_t i = 0; i < NI; ++i) {
     int64_t nv = 0, nt = 0;
     for (int64_t j = 0; j < N; ++j)
       for (int64_t k = 0; k < N; ++k) {
-        nv += __builtin_popcount(point_edges(S, N, i, j, k, iso));
-        if (i + 1 < N && j + 1 < N && k + 1 < N)
+        nv += __builtin_popcount(point_edges(S, NI, N, i, j, k, iso));
+        if (i + 1 < NI && j + 1 < N && k + 1 < N)
           nt += MPL_MC_TRI_COUNT[cell_case(S, N, i, j, k, iso)];
       }
     slab_verts[i] = nv;
@@ -69,11 +72,11 @@ void mpl_oracle_mc_count(const float* S, int64_t N, float iso, int64_t* slab_ver
   }
 }
 
-static float grad_axis(const float* S, int64_t N, const int64_t idx[3], int axis) {
+static float grad_axis(const float* S, int64_t NI, int64_t N, const int64_t idx[3], int axis) {
   int64_t lo[3] = {idx[0], idx[1], idx[2]};
   int64_t hi[3] = {idx[0], idx[1], idx[2]};
   if (idx[axis] > 0) lo[axis] -= 1;
-  if (idx[axis] + 1 < N) hi[axis] += 1;
+  if (idx[axis] + 1 < (axis == 0 ? NI : N)) hi[axis] += 1;
   float d = S[lin(N, hi[0], hi[1], hi[2])] - S[lin(N, lo[0], lo[1], lo[2])];
   return d / (float)(hi[axis] - lo[axis]);
 }
@@ -89,17 +92,17 @@ static inline int64_t vertex_id(const int64_t* vprefix, const uint8_t* vmask, in
 /* Emit vertices (xyz), normals, values and faces.  slab_vbase/slab_tbase are
  * exclusive prefix sums of the counts from mpl_oracle_mc_count.  Scratch:
  * vmask [N^3] bytes and vprefix [N^3] int64. */
-void mpl_oracle_mc_emit(const float* S, int64_t N, float iso, float vs, const float* origin,
-                        const int64_t* slab_vbase, const int64_t* slab_tbase, uint8_t* vmask,
-                        int64_t* vprefix, float* verts, float* normals, float* values,
-                        int32_t* faces) {
+void mpl_oracle_mc_emit(const float* S, int64_t NI, int64_t N, float iso, float vs,
+                        const float* origin, const int64_t* slab_vbase,
+                        const int64_t* slab_tbase, uint8_t* vmask, int64_t* vprefix,
+                        float* verts, float* normals, float* values, int32_t* faces) {
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t i = 0; i < N; ++i) {
+  for (int64_t i = 0; i < NI; ++i) {
     int64_t v = slab_vbase[i];
     for (int64_t j = 0; j < N; ++j)
       for (int64_t k = 0; k < N; ++k) {
         int64_t p = lin(N, i, j, k);
-        int m = point_edges(S, N, i, j, k, iso);
+        int m = point_edges(S, NI, N, i, j, k, iso);
         vmask[p] = (uint8_t)m;
         vprefix[p] = v;
         for (int a = 0; a < 3; ++a) {
@@ -118,8 +121,8 @@ void mpl_oracle_mc_emit(const float* S, int64_t N, float iso, float vs, const fl
           }
           float n[3];
           for (int d = 0; d < 3; ++d) {
-            float g0 = grad_axis(S, N, idx0, d);
-            float g1 = grad_axis(S, N, idx1, d);
+            float g0 = grad_axis(S, NI, N, idx0, d);
+            float g1 = grad_axis(S, NI, N, idx1, d);
             float dg = g1 - g0;
             float tg = t * dg;
             n[d] = g0 + tg;
@@ -136,7 +139,7 @@ void mpl_oracle_mc_emit(const float* S, int64_t N, float iso, float vs, const fl
   }
   /* faces need the vertex ids of the next slab too: second pass */
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t i = 0; i < N - 1; ++i) {
+  for (int64_t i = 0; i < NI - 1; ++i) {
     int64_t t = slab_tbase[i];
     for (int64_t j = 0; j + 1 < N; ++j)
       for (int64_t k = 0; k + 1 < N; ++k) {

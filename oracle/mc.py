@@ -42,8 +42,9 @@ def _load():
     if _lib is None:
         lib = ctypes.CDLL(build())
         P = ctypes.c_void_p
-        lib.mpl_oracle_mc_count.argtypes = [P, ctypes.c_int64, ctypes.c_float, P, P]
-        lib.mpl_oracle_mc_emit.argtypes = [P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+        I64 = ctypes.c_int64
+        lib.mpl_oracle_mc_count.argtypes = [P, I64, I64, ctypes.c_float, P, P]
+        lib.mpl_oracle_mc_emit.argtypes = [P, I64, I64, ctypes.c_float, ctypes.c_float,
                                            P, P, P, P, P, P, P, P, P]
         _lib = lib
     return _lib
@@ -54,14 +55,16 @@ def _ptr(a):
 
 
 def marching_cubes_raw(S, iso=0.0, voxel_size=1.0, origin=(0.0, 0.0, 0.0)):
-    """Canonical-order marching cubes of a C-order [N, N, N] float32 volume."""
+    """Canonical-order marching cubes of a C-order [N, N, N] float32 volume,
+    or of a slab [NI, N, N] of NI >= 2 consecutive i-planes of one (vertex
+    coordinates then count i from the slab's first plane)."""
     S = np.ascontiguousarray(S, np.float32)
-    N = S.shape[0]
-    assert S.shape == (N, N, N)
+    NI, N = S.shape[0], S.shape[1]
+    assert S.shape == (NI, N, N) and NI >= 1
     lib = _load()
-    sv = np.zeros(N, np.int64)
-    st = np.zeros(N, np.int64)
-    lib.mpl_oracle_mc_count(_ptr(S), N, ctypes.c_float(iso), _ptr(sv), _ptr(st))
+    sv = np.zeros(NI, np.int64)
+    st = np.zeros(NI, np.int64)
+    lib.mpl_oracle_mc_count(_ptr(S), NI, N, ctypes.c_float(iso), _ptr(sv), _ptr(st))
     vbase = np.concatenate([[0], np.cumsum(sv)[:-1]]).astype(np.int64)
     tbase = np.concatenate([[0], np.cumsum(st)[:-1]]).astype(np.int64)
     V, F = int(sv.sum()), int(st.sum())
@@ -69,10 +72,10 @@ def marching_cubes_raw(S, iso=0.0, voxel_size=1.0, origin=(0.0, 0.0, 0.0)):
     normals = np.zeros((V, 3), np.float32)
     values = np.zeros(V, np.float32)
     faces = np.zeros((F, 3), np.int32)
-    vmask = np.zeros(N ** 3, np.uint8)
-    vprefix = np.zeros(N ** 3, np.int64)
+    vmask = np.zeros(NI * N * N, np.uint8)
+    vprefix = np.zeros(NI * N * N, np.int64)
     org = np.asarray(origin, np.float32)
-    lib.mpl_oracle_mc_emit(_ptr(S), N, ctypes.c_float(iso), ctypes.c_float(voxel_size),
+    lib.mpl_oracle_mc_emit(_ptr(S), NI, N, ctypes.c_float(iso), ctypes.c_float(voxel_size),
                            _ptr(org), _ptr(vbase), _ptr(tbase), _ptr(vmask), _ptr(vprefix),
                            _ptr(verts), _ptr(normals), _ptr(values), _ptr(faces))
     return verts, faces, normals, values

@@ -19,7 +19,14 @@ made by the reference's own code.
   (tiny_three_level.npz, w0 = 30) over 10,000 seeded points near its zero
   set, in chunks of 4,096 and of 2^18; ``open3d`` (absent) is stubbed by a
   reader that returns those points, and ``i3d.meshing``'s ``plyfile`` and
-  ``skimage`` imports are stubbed.
+  ``skimage`` imports are stubbed;
+* ``multistage_increasing.npz``: the reference's create_mesh_multistage
+  (i3d/meshing.py:135-264) on the same model with band widths that grow
+  from one level to the next (0.005 then 0.05), 24^3 grid, chunks of 37
+  points (10 chunks stop after level 0: no point of theirs is in the first
+  band): the volume it hands to marching cubes and the points each residual
+  level evaluated.  Its CUDA stream synchronisation is shimmed to
+  a no-op (the loop runs on the CPU here).
 """
 
 from __future__ import annotations
@@ -117,6 +124,47 @@ def main():
         res[f"deltas_batch{batch}"] = np.array(
             ref_reconstruct.adaptive_deltas(models, "cloud.ply", "cpu", batch=batch), np.float64)
     np.savez_compressed(os.path.join(HERE, "adaptive_deltas.npz"), **res)
+
+    # band widths that grow: masks over whole chunks and the per-chunk break
+    from i3d import meshing
+    evaluated = [[] for _ in models]
+    captured = {}
+
+    class Rec(torch.nn.Module):
+        def __init__(self, m, i):
+            super().__init__()
+            self.m, self.i = m, i
+
+        def forward(self, x):
+            evaluated[self.i].append(x.detach().clone())
+            return self.m(x)
+
+    class NoSync:
+        def synchronize(self):
+            return None
+
+    orig_stream, orig_conv = torch.cuda.current_stream, meshing.convert_sdf_samples_to_ply
+
+    def conv(vol, *a, **k):
+        captured["volume"] = np.array(vol, copy=True)
+        return np.zeros((0, 3)), np.zeros((0, 3), np.int64), np.zeros((0, 3)), np.zeros(0)
+
+    torch.cuda.current_stream = lambda *a, **k: NoSync()
+    meshing.convert_sdf_samples_to_ply = conv
+    N, deltas, chunk = 24, [0.005, 0.05], 37  # 10 of 374 chunks break after level 0
+    try:
+        meshing.create_mesh_multistage([Rec(m, i) for i, m in enumerate(models)], deltas=deltas,
+                                       N=N, max_batch=chunk, device="cpu", silent=True)
+    finally:
+        torch.cuda.current_stream = orig_stream
+        meshing.convert_sdf_samples_to_ply = orig_conv
+    inc = {"N": np.array(N), "deltas": np.array(deltas), "chunk": np.array(chunk),
+           "S": captured["volume"].reshape(-1)}
+    for i in (1, 2):
+        inc[f"band{i}_pts"] = torch.cat(evaluated[i]).numpy() if evaluated[i] else \
+            np.zeros((0, 3), np.float32)
+    np.savez_compressed(os.path.join(HERE, "multistage_increasing.npz"), **inc)
+    print("increasing bands: evaluated", [inc[f"band{i}_pts"].shape[0] for i in (1, 2)])
     print("loaders:", out[:3], "adaptive deltas:", res["deltas_batch4096"],
           res["deltas_batch262144"])
 

@@ -132,3 +132,33 @@ def test_create_mesh_single_level_drop_in(lib, tmp_path):
         assert np.array_equal(a, b)
     head = open(path, "rb").read().split(b"end_header\n")[0].decode()
     assert f"element vertex {verts.shape[0]}" in head and f"element face {faces.shape[0]}" in head
+
+
+def test_growing_band_widths_match_reference(lib):
+    """Band widths that grow (0.005 then 0.05) over chunks of 37 points: the
+    reference's masks cover whole chunks, and 10 chunks stop after level 0.
+    The volume is within 1e-5 of the reference's, and each residual level
+    evaluated exactly the reference's points."""
+    from mplicits_gb300.meshing import BandedReconstruction, create_mesh_multistage
+    _, sds, _ = tiny_levels()
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "multistage_increasing.npz"))
+    N, chunk = int(g["N"]), int(g["chunk"])
+    deltas = [float(x) for x in g["deltas"]]
+    rec = BandedReconstruction(_models(sds), deltas, N, "cuda", chunk=chunk)
+    assert not rec.nested
+    S = rec.sample().cpu().numpy()
+    assert np.abs(S - g["S"]).max() <= 1e-5
+    grid = siren.grid_coords(N, 2.0 / (N - 1))
+    sizes = rec.band_sizes()
+    for i in (1, 2):
+        idx = rec.band_index[i - 1][:sizes[i - 1]].cpu().numpy()
+        assert idx.shape[0] == g[f"band{i}_pts"].shape[0], i
+        got = {tuple(r) for r in grid[idx].tolist()}
+        ref = {tuple(r) for r in g[f"band{i}_pts"].tolist()}
+        assert got == ref, i
+    # the drop-in passes max_batch through as the chunk
+    verts, faces, _, _, _ = create_mesh_multistage(_models(sds), deltas, N=N, max_batch=chunk,
+                                                   device="cuda", silent=True)
+    v2, f2, _, _ = mc.marching_cubes_raw(S.reshape(N, N, N), 0.0, np.float32(2.0 / (N - 1)),
+                                         (-1, -1, -1))
+    assert np.array_equal(faces, f2) and np.array_equal(verts, v2)

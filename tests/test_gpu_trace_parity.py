@@ -79,7 +79,14 @@ def test_trace_init_matches_oracle_rays(lib, cam_i, eye_inside):
     assert not differ[np.abs(disc) > 1e-5].any()
     both = (st == 0) & (s_ref == 0)
     assert both.sum() > P // 20
-    assert np.abs(o[both] - o_ref[both]).max() <= 2e-5
+    # entry points: t = -b - sqrt(disc) loses accuracy as disc -> 0 (a ray
+    # that grazes the sphere), so the position bound holds where disc is not
+    # small; every entry point lies on the sphere to float32 rounding
+    good = both & (disc > 1e-2)
+    assert good.sum() > both.sum() // 2
+    assert np.abs(o[good] - o_ref[good]).max() <= 2e-5
+    if not eye_inside:
+        assert np.abs(np.linalg.norm(o[both], axis=1) - 1.2).max() <= 2e-6
     if eye_inside:
         assert (st == 0).all() and np.array_equal(o, np.broadcast_to(np.float32(eye), o.shape))
     n = int(count.item())
@@ -105,8 +112,10 @@ def test_full_frame_matches_oracle(lib, precision, tail_from, graph, cam_i):
     pixel.  For the rays whose final state agrees:
       * a GPU hit is a hit of the float64 function: |S64(p_gpu)| <= eps + e,
         e the bound of the precision's SDF error;
-      * along the ray it lies where the oracle's does: |p_gpu - p64| |n.d| <=
-        2 (eps + e) (first order in the distance to the surface);
+      * where the ray meets the surface at an angle (|n.d| >= 0.3), the hit
+        lies where the oracle's does: |p_gpu - p64| |n.d| <= 2 (eps + e)
+        (first order in the distance to the surface; a grazing ray can
+        legitimately stop at another point within eps + e of the surface);
       * its normal is the float64 band-gated gradient at p_gpu.
     The BF16 frame runs as the benchmark runs it (persistent tail from step
     32, graph replay)."""
@@ -134,17 +143,20 @@ def test_full_frame_matches_oracle(lib, precision, tail_from, graph, cam_i):
     for i, dlt in enumerate(DELTAS):
         gate_ok &= np.abs(np.abs(partial[i]) - dlt) > 2 * e
     gerr = (np.linalg.norm(G[hit] - g64, axis=1) / np.linalg.norm(g64, axis=1))[gate_ok]
+    steep = cos >= 0.3
     stats = {"precision": precision, "cam": cam_i, "rays": int(pix.size), "agree": agree,
              "hits": int(hit.sum()), "S64_at_gpu_hit_max": float(np.abs(S64).max()),
-             "pos_err_weighted_max": float(pos_err.max()),
+             "pos_err_weighted_max": float(pos_err[steep].max()),
+             "pos_err_weighted_max_all": float(pos_err.max()), "steep": int(steep.sum()),
              "normal_rel_err_max": float(gerr.max()), "normal_rel_err_median":
              float(np.median(gerr)), "gated_out": int((~gate_ok).sum())}
     print("TRACE_PARITY", json.dumps(stats))
     assert hit.sum() > 1000
-    assert agree >= (0.995 if precision == "fp32" else 0.98), stats
+    assert agree >= 0.995, stats
     assert np.abs(S64).max() <= EPS + e, stats
-    assert pos_err.max() <= 2 * (EPS + e), stats
-    assert gerr.max() <= (1e-3 if precision == "fp32" else 0.1), stats
+    assert steep.sum() > hit.sum() // 2
+    assert pos_err[steep].max() <= 2 * (EPS + e), stats
+    assert gerr.max() <= (1e-4 if precision == "fp32" else 0.05), stats
 
 
 @pytest.mark.parametrize("mode", [0, 1])
