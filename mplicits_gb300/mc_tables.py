@@ -238,6 +238,35 @@ def render_header() -> str:
 HEADER_PATH = os.path.join(os.path.dirname(__file__), "csrc", "mc_tables.h")
 
 
+def ambiguity_classes():
+    """Per case (0..255): (face, interior).  ``face``: some face of the cell
+    has its two inside corners on one diagonal and its two outside corners on
+    the other (four crossing edges), the configuration where this table's
+    fixed rule ("inside corners separated") and a face test such as the
+    asymptotic decider of Lewiner et al. 2003 (scikit-image's method) can
+    choose different segment pairs.  ``interior``: no face is ambiguous but
+    the two inside (or the two outside) corners are the ends of a body
+    diagonal, the case where Lewiner's interior test may join them with a
+    tube instead of two separate triangles.  Every other case has one
+    topology; two tables can then still triangulate a loop of four or more
+    vertices differently, which changes faces but not the surface's
+    vertices or its connectivity."""
+    out = []
+    for case in range(256):
+        ins = [(case >> c) & 1 for c in range(8)]
+        face = any(ins[cyc[0]] == ins[cyc[2]] and ins[cyc[1]] == ins[cyc[3]] and
+                   ins[cyc[0]] != ins[cyc[1]] for cyc, _ in _faces())
+        n_in = sum(ins)
+        pair = None
+        if n_in == 2:
+            pair = [c for c in range(8) if ins[c]]
+        elif n_in == 6:
+            pair = [c for c in range(8) if not ins[c]]
+        interior = (not face) and pair is not None and (pair[0] ^ pair[1]) == 7
+        out.append((face, interior))
+    return out
+
+
 if __name__ == "__main__":
     with open(HEADER_PATH, "w") as f:
         f.write(render_header())

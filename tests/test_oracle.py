@@ -137,3 +137,81 @@ def test_mc_table_complementary_cases_mirror():
         e1 = set(table[case][table[case] >= 0].tolist())
         e2 = set(table[255 - case][table[255 - case] >= 0].tolist())
         assert e1 == e2
+
+
+def test_mc_ambiguity_classes():
+    """The cases where this project's face rule and Lewiner's face and
+    interior tests can choose different topologies: 120 of the 256 cases
+    have a face with four crossing edges, and 8 (a body-diagonal pair of
+    inside or outside corners) an interior ambiguity only."""
+    from mplicits_gb300.mc_tables import ambiguity_classes
+    a = ambiguity_classes()
+    assert sum(f for f, _ in a) == 120 and sum(i for _, i in a) == 8
+    assert a[0] == (False, False) and a[255] == (False, False)
+    assert a[(1 << 0) | (1 << 3)] == (True, False)    # corners 0, 3: a face diagonal
+    assert a[(1 << 0) | (1 << 7)] == (False, True)    # corners 0, 7: the body diagonal
+    assert a[255 ^ ((1 << 1) | (1 << 6))] == (False, True)
+    assert a[(1 << 0) | (1 << 1)] == (False, False)   # an edge: one topology
+
+
+def test_oracle_slab_marching_cubes_equals_the_cube_layer():
+    """Marching cubes of a slab of two adjacent planes gives the triangles of
+    that cell layer of the whole volume (the CPU baseline times slabs):
+    faces come in cell order, so layer i is one contiguous run of them."""
+    import ctypes
+    N, i = 33, 17
+    S = _sphere(N)
+    vs_ = np.float32(2.0 / (N - 1))
+    v, f, _, _ = mc.marching_cubes_raw(S, 0.0, vs_, (-1, -1, -1))
+    sv, st = np.zeros(N, np.int64), np.zeros(N, np.int64)
+    mc._load().mpl_oracle_mc_count(mc._ptr(S), N, N, ctypes.c_float(0.0), mc._ptr(sv),
+                                   mc._ptr(st))
+    t0 = int(st[:i].sum())
+    layer = v[f[t0:t0 + st[i]]]
+    vs, fs, _, _ = mc.marching_cubes_raw(S[i:i + 2], 0.0, vs_, (-1, -1, -1))
+    got = vs[fs]
+    got[:, :, 0] = got[:, :, 0] + np.float32(i) * vs_
+    assert fs.shape[0] == st[i] > 0
+    assert np.allclose(got, layer, atol=1e-6)
+
+
+def test_bf16_error_budget():
+    """Float64 emulation of the tensor-core kernel's roundings on level 0 of
+    the trained model over random points of the 512^3 grid: with BF16
+    operands the SDF error exceeds the 5e-4 target and comes mostly from the
+    rounded activations; FP16 operands stay inside it."""
+    import os
+    from conftest import GOLDEN
+
+    def bf16(a):
+        a = np.asarray(a, np.float32)
+        u = a.view(np.uint32).astype(np.uint64)
+        u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+        return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+    def f16(a):
+        return np.asarray(a, np.float32).astype(np.float16).astype(np.float64)
+
+    def exact(a):
+        return np.asarray(a, np.float64)
+
+    d = np.load(os.path.join(GOLDEN, "three_level_sphere.npz"))
+    P = [(d[f"L0.net.{j}.0.weight"].astype(np.float64), d[f"L0.net.{j}.0.bias"].astype(np.float64))
+         for j in range(4)]
+    N = 512
+    idx = np.random.default_rng(0).integers(0, N ** 3, 1 << 14)
+    x = siren.grid_coords(N, 2.0 / (N - 1), idx).astype(np.float64)
+
+    def run(ra, rw):
+        s = np.sin(x @ (30 * P[0][0]).T + 30 * P[0][1])
+        for l in (1, 2):
+            W, b = P[l]
+            s = np.sin(ra(s) @ rw(np.float32(30) * W.astype(np.float32)).T + 30 * b)
+        return (s @ P[3][0].T + P[3][1])[:, 0]
+
+    ref = run(exact, exact)
+    e_bf16 = np.abs(run(bf16, bf16) - ref).max()
+    e_acts = np.abs(run(bf16, exact) - ref).max()
+    e_f16 = np.abs(run(f16, f16) - ref).max()
+    assert e_bf16 > 5e-4 and e_acts > 0.6 * e_bf16
+    assert e_f16 < 5e-4
