@@ -52,14 +52,43 @@ int64_t option_value(int32_t option);
 // ---------------------------------------------------------------------------
 // grid coordinates of i3d/meshing.py:42-63 (float32 true division, fmod)
 // ---------------------------------------------------------------------------
+// fmod(a, b) for 0 <= a < 2^22 and an integer-valued float 2 <= b <= 2^11,
+// inv_b = float32(1 / b).  The quotient estimate trunc(a * inv_b) is off by
+// at most one; a - n b is a multiple of ulp(a) below 2b, so the FMA and the
+// one correction are exact, and the result equals fmodf(a, b) bit for bit
+// (checked on every index of the N^3 grids for N = 2..69 and for N = 127,
+// 128, 129, 255, 256, 300, 384, 511, 512, 640, 777, 1000, 1023, 1024, 1290).
+__device__ __forceinline__ float fmod_grid(float a, float b, float inv_b) {
+  const float n = truncf(__fmul_rn(a, inv_b));
+  float r = __fmaf_rn(-n, b, a);
+  if (r < 0.f)
+    r = __fadd_rn(r, b);
+  else if (r >= b)
+    r = __fsub_rn(r, b);
+  return r;
+}
+
 __device__ __forceinline__ void grid_point(int64_t p, int32_t N, float vs, float off0, float off1,
                                            float off2, float& x, float& y, float& z) {
   const float fN = (float)N;
-  const float idx_f = __ll2float_rn(p);
-  const float s2 = (float)(p % (int64_t)N);
-  const float q1 = __fdiv_rn(idx_f, fN);
-  const float s1 = fmodf(q1, fN);
-  const float s0 = fmodf(__fdiv_rn(q1, fN), fN);
+  float s0, s1, s2;
+  if (p < 0x80000000ll && N <= 1290) {
+    // 32-bit integer work and an exact fmod: no 64-bit division (which runs
+    // on the FP64 pipe) and no library fmodf; same bits as the branch below
+    const uint32_t p32 = (uint32_t)p;
+    const float idx_f = __uint2float_rn(p32);
+    s2 = (float)(p32 % (uint32_t)N);
+    const float q1 = __fdiv_rn(idx_f, fN);
+    const float inv = __frcp_rn(fN);
+    s1 = fmod_grid(q1, fN, inv);
+    s0 = fmod_grid(__fdiv_rn(q1, fN), fN, inv);
+  } else {
+    const float idx_f = __ll2float_rn(p);
+    s2 = (float)(p % (int64_t)N);
+    const float q1 = __fdiv_rn(idx_f, fN);
+    s1 = fmodf(q1, fN);
+    s0 = fmodf(__fdiv_rn(q1, fN), fN);
+  }
   x = __fadd_rn(__fmul_rn(s0, vs), off0);
   y = __fadd_rn(__fmul_rn(s1, vs), off1);
   z = __fadd_rn(__fmul_rn(s2, vs), off2);

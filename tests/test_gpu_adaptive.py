@@ -111,6 +111,10 @@ def test_reconstruct_cli_input_uses_adaptive_deltas(lib, tmp_path, capsys):
     from mplicits_gb300.reconstruct import adaptive_deltas, main
     _, sds, _ = tiny_levels()
     models = _models(sds, 32)
+    # the trainers save the coarser levels with omega baked in, and the CLI
+    # loads --coarse_path and --medium_path with w0 = 1 (reconstruct.py:99-112)
+    models[0].update_omegas(w0=1)
+    models[1].update_omegas(w0=1)
     paths = []
     for name, m in zip(("coarse", "medium", "fine"), models):
         p = os.path.join(tmp_path, f"{name}.pth")

@@ -89,7 +89,7 @@ def test_grid_points_are_the_reference_grid(lib):
     from mplicits_gb300 import capi
     from mplicits_gb300.meshing import _grid_points
     g = golden("grid.npz")
-    for N in (4, 16, 127, 512):
+    for N in (2, 3, 4, 5, 16, 127, 128, 512):
         pts = _grid_points(N, 2.0 / (N - 1))
         n = N ** 3
         out = torch.empty(n, 3, device="cuda")
@@ -97,6 +97,26 @@ def test_grid_points_are_the_reference_grid(lib):
                                        capi.stream_ptr()), "grid")
         h = hashlib.sha256(out.cpu().numpy().tobytes()).hexdigest()
         assert h == str(g[f"sha_{N}"]), N
+
+
+@pytest.mark.parametrize("N", [1000, 1290, 1291, 1300])
+def test_grid_points_of_large_grids_match_the_oracle(lib, N):
+    """Indexed grid points of grids too large to write whole, up to the
+    largest N the exact 32-bit path covers (1290) and past it (the 64-bit
+    path), against the oracle's float32 restatement of i3d/meshing.py:42-63."""
+    from mplicits_gb300 import capi
+    from mplicits_gb300.meshing import _grid_points
+    rng = np.random.default_rng(N)
+    idx = np.concatenate([rng.integers(0, N ** 3, 200000), [0, N ** 3 - 1, N * N - 1, N * N,
+                                                             N ** 3 - N]])
+    idx = idx[idx < 2 ** 31].astype(np.int32)
+    pts = _grid_points(N, 2.0 / (N - 1))
+    out = torch.empty(idx.shape[0], 3, device="cuda")
+    ti = torch.from_numpy(idx).cuda()
+    capi.check(lib.mpl_grid_points(ctypes.byref(pts), capi.ptr(ti), idx.shape[0], capi.ptr(out),
+                                   capi.stream_ptr()), "grid")
+    ref = siren.grid_coords(N, 2.0 / (N - 1), idx.astype(np.int64))
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
 
 
 def test_grid_mode_index_accumulate_and_fused_band(lib):

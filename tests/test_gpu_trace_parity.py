@@ -112,10 +112,10 @@ def test_full_frame_matches_oracle(lib, precision, tail_from, graph, cam_i):
     pixel.  For the rays whose final state agrees:
       * a GPU hit is a hit of the float64 function: |S64(p_gpu)| <= eps + e,
         e the bound of the precision's SDF error;
-      * where the ray meets the surface at an angle (|n.d| >= 0.3), the hit
-        lies where the oracle's does: |p_gpu - p64| |n.d| <= 2 (eps + e)
-        (first order in the distance to the surface; a grazing ray can
-        legitimately stop at another point within eps + e of the surface);
+      * where the ray meets the surface at an angle (|n.d| >= 0.3 at both
+        hits), the hit lies where the oracle's does: |p_gpu - p64| |n.d| <=
+        2 (eps + e) (first order in the distance to the surface; a grazing
+        ray can legitimately stop at another point within eps + e of it);
       * its normal is the float64 band-gated gradient at p_gpu.
     The BF16 frame runs as the benchmark runs it (persistent tail from step
     32, graph replay)."""
@@ -135,7 +135,11 @@ def test_full_frame_matches_oracle(lib, precision, tail_from, graph, cam_i):
     g64, S64, partial = otrace.banded_gradient(levels, DELTAS, org[hit])
     _, d_ref, _ = otrace.camera_rays(cam, pixels=pix[hit])
     nrm = g_ref[hit] / np.linalg.norm(g_ref[hit], axis=1, keepdims=True)
-    cos = np.abs((nrm * d_ref).sum(1))
+    ngpu = G[hit] / np.linalg.norm(G[hit], axis=1, keepdims=True)
+    # the angle at both hits: a ray can pass a bump within the tensor-core
+    # error of the surface (a grazing stop for one arithmetic) and reach a
+    # steep hit behind it (for the other)
+    cos = np.minimum(np.abs((nrm * d_ref).sum(1)), np.abs((ngpu * d_ref).sum(1)))
     pos_err = np.linalg.norm(org[hit] - o_ref[hit], axis=1) * cos
     # rays whose gating at p_gpu is within the error of a band threshold may
     # legitimately sum different levels; compare the normal elsewhere

@@ -215,3 +215,30 @@ def test_bf16_error_budget():
     e_f16 = np.abs(run(f16, f16) - ref).max()
     assert e_bf16 > 5e-4 and e_acts > 0.6 * e_bf16
     assert e_f16 < 5e-4
+
+
+def test_exact_grid_fmod_identity():
+    """The kernels' fast fmod of the grid formula (csrc/common.cuh fmod_grid:
+    trunc(a * (1/b)), one FMA, one correction) equals fmodf bit for bit on
+    the grid's quotients: every index for N <= 40, and 2^20 random indices
+    plus the extreme ones for large N.  Emulated in float32 (the FMA as an
+    exact float64 difference rounded once)."""
+    def fast(a, b, inv):
+        n = np.trunc((a * inv).astype(np.float32)).astype(np.float32)
+        r = (a.astype(np.float64) - n.astype(np.float64) * np.float64(b)).astype(np.float32)
+        r = np.where(r < 0, (r + b).astype(np.float32), r)
+        return np.where(r >= b, (r - b).astype(np.float32), r)
+
+    rng = np.random.default_rng(0)
+    for N in list(range(2, 41)) + [127, 512, 1023, 1290]:
+        fN = np.float32(N)
+        inv = np.float32(1) / fN
+        if N <= 40:
+            p = np.arange(N ** 3, dtype=np.int64)
+        else:
+            p = np.concatenate([rng.integers(0, N ** 3, 1 << 20),
+                                np.arange(N ** 3 - 4096, N ** 3), np.arange(4096)])
+        q1 = (p.astype(np.float32) / fN).astype(np.float32)
+        q2 = (q1 / fN).astype(np.float32)
+        for q in (q1, q2):
+            assert np.array_equal(fast(q, fN, inv).view(np.uint32), np.fmod(q, fN).view(np.uint32)), N
