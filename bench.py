@@ -704,11 +704,12 @@ def batch_bench(device, K, W):
         return a.elapsed_time(b) / k
 
     ms_batch = timed(bl.replay, K, W)
+    old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
     capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, cfg.epilogue_unit)
     try:
         ms_bf16 = timed(lambda: per_level("bf16"), K, W)
     finally:
-        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 16)
+        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
     ms_fp32 = timed(lambda: per_level("fp32"), 1, 1)
     peak_tf, _, src = peaks()
     widths = [e.model.linears()[0].out_features for e in entries[::3]]

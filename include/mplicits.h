@@ -461,17 +461,24 @@ int mpl_batch_autotune(const MplBatchPlan* plan, int32_t repeats, MplBatchConfig
 /* Process-wide kernel options (read at each launch). */
 enum {
   MPL_OPT_BF16_EPILOGUE_UNIT = 1, /* features per epilogue warp and 64-wide chunk of
-                                     the BF16 level kernel: 16 (16 epilogue warps,
-                                     default) or 32 (8 warps)                    */
+                                     the tensor-core level kernels and the tracing
+                                     tail: 32 (8 epilogue warps, default) or 16
+                                     (16 warps); the output dot's partial sums
+                                     follow the unit, so roundings differ        */
   MPL_OPT_TC_TILES_IN_FLIGHT = 2, /* tiles per CTA of the tensor-core level kernel:
                                      2 (default; GEMMs of one tile overlap the
                                      epilogue of the other, results identical) or
                                      1 (single-tile kernel)                      */
-  MPL_OPT_TC_GRAD_REVERSE = 3     /* input gradient on the tensor cores: 1
+  MPL_OPT_TC_GRAD_REVERSE = 3,    /* input gradient on the tensor cores: 1
                                      (default) a backward sweep over each tile of
                                      128 points (levels with one or two hidden
                                      GEMMs), 0 forward-mode tangent rows (4 rows
                                      per point); values equal, roundings differ  */
+  MPL_OPT_TC_LAYER0_WARPS = 4     /* first layer of the two-tile kernel: 8
+                                     (default) or 4 warps of its own, handing the
+                                     first GEMM its A operand chunk by chunk, or 0
+                                     (computed in the epilogue's last drain of the
+                                     previous tile); results identical           */
 };
 int mpl_set_option(int32_t option, int64_t value);
 int mpl_get_option(int32_t option, int64_t* value);

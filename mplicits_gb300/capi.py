@@ -35,6 +35,7 @@ PRECISIONS = {"fp32": MPL_FP32, "bf16": MPL_BF16, "fp16": MPL_F16}
 MPL_OPT_BF16_EPILOGUE_UNIT = 1
 MPL_OPT_TC_TILES_IN_FLIGHT = 2
 MPL_OPT_TC_GRAD_REVERSE = 3
+MPL_OPT_TC_LAYER0_WARPS = 4
 MPL_BATCH_NEIGH_DELTA = 1
 MPL_BATCH_DITHER = 2
 

@@ -40,15 +40,17 @@ int sm_count() {
   return cached[dev];
 }
 
-static int64_t g_opt_bf16_unit = 16;
+static int64_t g_opt_bf16_unit = 32;
 static int64_t g_opt_tc_tiles = 2;
 static int64_t g_opt_grad_reverse = 1;
+static int64_t g_opt_layer0_warps = 8;
 
 int64_t option_value(int32_t option) {
   switch (option) {
     case MPL_OPT_BF16_EPILOGUE_UNIT: return g_opt_bf16_unit;
     case MPL_OPT_TC_TILES_IN_FLIGHT: return g_opt_tc_tiles;
     case MPL_OPT_TC_GRAD_REVERSE: return g_opt_grad_reverse;
+    case MPL_OPT_TC_LAYER0_WARPS: return g_opt_layer0_warps;
     default: return 0;
   }
 }
@@ -71,6 +73,10 @@ extern "C" int mpl_set_option(int32_t option, int64_t value) {
       if (value != 0 && value != 1) return MPL_ERR_INVALID_ARG;
       g_opt_grad_reverse = value;
       return MPL_OK;
+    case MPL_OPT_TC_LAYER0_WARPS:
+      if (value != 0 && value != 4 && value != 8) return MPL_ERR_INVALID_ARG;
+      g_opt_layer0_warps = value;
+      return MPL_OK;
     default:
       return MPL_ERR_INVALID_ARG;
   }
@@ -79,7 +85,7 @@ extern "C" int mpl_set_option(int32_t option, int64_t value) {
 extern "C" int mpl_get_option(int32_t option, int64_t* value) {
   if (!value) return MPL_ERR_INVALID_ARG;
   if (option != MPL_OPT_BF16_EPILOGUE_UNIT && option != MPL_OPT_TC_TILES_IN_FLIGHT &&
-      option != MPL_OPT_TC_GRAD_REVERSE)
+      option != MPL_OPT_TC_GRAD_REVERSE && option != MPL_OPT_TC_LAYER0_WARPS)
     return MPL_ERR_INVALID_ARG;
   *value = option_value(option);
   return MPL_OK;

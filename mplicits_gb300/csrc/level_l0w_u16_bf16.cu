@@ -1,0 +1,10 @@
+// Two-tile tensor-core level kernels with first-layer warps (4 or 8):
+// 16-feature epilogue units, BF16 operands.
+#include "level_l0w.cuh"
+
+namespace mpl {
+int launch_level_l0w_u16_bf16(const LevelArgs& a, int layer0_warps, cudaStream_t s) {
+  return layer0_warps == 8 ? l0w::launch_unit<16, 8, __nv_bfloat16>(a, s)
+                           : l0w::launch_unit<16, 4, __nv_bfloat16>(a, s);
+}
+}  // namespace mpl

@@ -390,9 +390,8 @@ __global__ void __launch_bounds__(bf16::Epi<U>::kThreads, 1) trace_march_kernel(
   if (warp == kMmaWarp) tc::tmem_dealloc(tmem, WP);
 }
 
-template <int WP, typename T>
-int launch(const Args& a, cudaStream_t s) {
-  constexpr int U = 16;
+template <int WP, int U, typename T>
+int launch_u(const Args& a, cudaStream_t s) {
   using C = Cfg<WP, U>;
   const size_t smem = C::bytes(a.levels, a.lay[0].nh);
   if (smem > 227 * 1024) return MPL_ERR_UNSUPPORTED;
@@ -405,6 +404,14 @@ int launch(const Args& a, cudaStream_t s) {
   trace_march_kernel<WP, U, T><<<(unsigned)grid, bf16::Epi<U>::kThreads, smem, s>>>(a);
   MPL_LAUNCH_CHECK();
   return MPL_OK;
+}
+
+// the epilogue unit width of the level launches (MPL_OPT_BF16_EPILOGUE_UNIT),
+// so that every ray gets the arithmetic of the launch-per-level loop
+template <int WP, typename T>
+int launch(const Args& a, cudaStream_t s) {
+  return option_value(MPL_OPT_BF16_EPILOGUE_UNIT) == 32 ? launch_u<WP, 32, T>(a, s)
+                                                         : launch_u<WP, 16, T>(a, s);
 }
 
 }  // namespace march

@@ -74,6 +74,7 @@ def test_batched_launch_equals_single_level_launches(lib, precision, unit, stage
     from mplicits_gb300.batch import BatchedLevels
     entries, _ = _entries(precision)
     init = [e.S.clone() for e in entries]
+    old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
     capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, unit)
     try:
         ref = _single(entries, precision)
@@ -81,7 +82,7 @@ def test_batched_launch_equals_single_level_launches(lib, precision, unit, stage
         bl.run(capi.MplBatchConfig(epilogue_unit=unit, stages=stages))
         torch.cuda.synchronize()
     finally:
-        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 16)
+        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
     assert capi.device_status() == capi.MPL_OK
     for i, (e, r) in enumerate(zip(entries, ref)):
         assert torch.equal(e.S, r), i
@@ -118,11 +119,12 @@ def test_autotune_and_graph_replay(lib):
     assert cfg.epilogue_unit in (16, 32) and cfg.stages in (2, 3) and ms > 0
     for e in entries:
         e.S.fill_(-3.0)
+    old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
     capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, cfg.epilogue_unit)
     try:
         ref = _single(entries, "bf16")
     finally:
-        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 16)
+        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
     bl.capture()
     bl.replay()
     torch.cuda.synchronize()

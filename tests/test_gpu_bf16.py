@@ -140,14 +140,55 @@ def test_two_tile_kernel_equals_single_tile_kernel(lib, epilogue_unit, cfg, P, p
     rng = np.random.default_rng(P + 1)
     x = torch.from_numpy(rng.uniform(-1, 1, (P, 3)).astype(np.float32)).cuda()
     out = {}
-    for tiles in (1, 2):
+    # single tile; two tiles with the first layer in the drains; two tiles
+    # with first-layer warps.  Gradients in forward mode (the tangent rows of
+    # these kernels) and in reverse mode.
+    for tiles, l0w in ((1, 0), (2, 0), (2, 4), (2, 8)):
         capi.set_option(capi.MPL_OPT_TC_TILES_IN_FLIGHT, tiles)
+        capi.set_option(capi.MPL_OPT_TC_LAYER0_WARPS, l0w)
         try:
             S = level_forward(m, x, precision=prec).clone()
             Sg, G = level_gradient(m, x, precision=prec)
-            out[tiles] = (S, Sg.clone(), G.clone())
+            capi.set_option(capi.MPL_OPT_TC_GRAD_REVERSE, 0)
+            Sf, Gf = level_gradient(m, x, precision=prec)
+            out[(tiles, l0w)] = (S, Sg.clone(), G.clone(), Sf.clone(), Gf.clone())
         finally:
             capi.set_option(capi.MPL_OPT_TC_TILES_IN_FLIGHT, 2)
-    for a, b in zip(out[1], out[2]):
-        assert torch.equal(a, b)
+            capi.set_option(capi.MPL_OPT_TC_LAYER0_WARPS, 8)
+            capi.set_option(capi.MPL_OPT_TC_GRAD_REVERSE, 1)
+    for k in ((2, 0), (2, 4), (2, 8)):
+        for a, b in zip(out[(1, 0)], out[k]):
+            assert torch.equal(a, b), k
+    assert capi.device_status() == capi.MPL_OK
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("N", [40, 97, 128])
+def test_layer0_warps_grid_bands_and_point_lists(lib, epilogue_unit, prec, N):
+    """The first-layer-warp kernel against the kernel that computes the
+    first layer in its drains, on the paths the reconstruction takes: grid
+    points with a fused band list, then index lists whose count lives on the
+    device, accumulating into S.  Values and band lists are identical."""
+    from mplicits_gb300 import capi
+    from mplicits_gb300.meshing import BandedReconstruction
+    levels = [_model([256, 256, 256], 31 + i)[0] for i in range(3)]
+    for lv, sc in zip(levels[1:], (0.1, 0.02)):
+        with torch.no_grad():
+            lv.net[-1][0].weight.mul_(sc)
+    res = {}
+    for l0w in (0, 4, 8):
+        capi.set_option(capi.MPL_OPT_TC_LAYER0_WARPS, l0w)
+        try:
+            rec = BandedReconstruction(levels, [0.3, 0.1], N, "cuda", prec)
+            rec.sample()
+            sizes = rec.band_sizes()
+            bands = [torch.sort(rec.band_index[i][:sizes[i]])[0] for i in range(2)]
+            res[l0w] = (rec.S.clone(), bands, sizes)
+        finally:
+            capi.set_option(capi.MPL_OPT_TC_LAYER0_WARPS, 8)
+    for k in (4, 8):
+        assert res[0][2] == res[k][2] and min(res[0][2]) > 0
+        assert torch.equal(res[0][0], res[k][0])
+        for a, b in zip(res[0][1], res[k][1]):
+            assert torch.equal(a, b)
     assert capi.device_status() == capi.MPL_OK

@@ -46,6 +46,7 @@ def test_fp32_gradient_vs_fp64(lib, cfg, P):
 @pytest.mark.parametrize("cfg", [[256, 256, 256], [128, 128, 128], [64, 64]])
 def test_bf16_gradient_vs_fp64(lib, cfg, unit):
     from mplicits_gb300 import capi
+    old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
     capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, unit)
     from mplicits_gb300.grad import level_gradient
     m, params = _model(cfg, 5, precision="bf16")
@@ -58,7 +59,7 @@ def test_bf16_gradient_vs_fp64(lib, cfg, unit):
     f64 = siren.siren_forward(params, m.omegas(), x, np.float64)
     assert np.abs(S.cpu().numpy() - f64).max() <= 5e-3
     assert capi.device_status() == capi.MPL_OK
-    capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 16)
+    capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
 
 
 def test_autograd_input_gradient_through_forward(lib):
