@@ -391,9 +391,8 @@ int launch_cfg(const LevelArgs& a, cudaStream_t s) {
 // the deepest weight ring that fits; MPL_ERR_UNSUPPORTED when the level has
 // more than two hidden GEMMs or its constants do not fit (the caller falls
 // back to the forward-mode gradient)
-template <int WP, typename T>
+template <int WP, int U, typename T>
 int launch_wp(const LevelArgs& a, cudaStream_t s) {
-  constexpr int U = 16;
   constexpr size_t kLimit = 227 * 1024;
   if (a.lay.nh < 1 || a.lay.nh > 2) return MPL_ERR_UNSUPPORTED;
   if (Cfg<WP, 4, U>::bytes(a.lay.nh) <= kLimit) return launch_cfg<WP, 4, U, T>(a, s);
@@ -402,12 +401,14 @@ int launch_wp(const LevelArgs& a, cudaStream_t s) {
   return MPL_ERR_UNSUPPORTED;
 }
 
-template <typename T>
+// U: the epilogue unit width of the forward kernels (MPL_OPT_BF16_EPILOGUE_UNIT),
+// whose output-dot partial sums S must equal bit for bit
+template <int U, typename T>
 int launch(const LevelArgs& a, cudaStream_t s) {
   switch (a.lay.WP) {
-    case 64: return launch_wp<64, T>(a, s);
-    case 128: return launch_wp<128, T>(a, s);
-    case 256: return launch_wp<256, T>(a, s);
+    case 64: return launch_wp<64, U, T>(a, s);
+    case 128: return launch_wp<128, U, T>(a, s);
+    case 256: return launch_wp<256, U, T>(a, s);
     default: return MPL_ERR_UNSUPPORTED;
   }
 }
