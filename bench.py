@@ -872,7 +872,7 @@ def main():
     achieved_tf = FLOP_PER_POINT * N ** 3 / (l0_ms * 1e-3) / 1e12
     traffic = None
     kernel_name = "level 0 tensor-core launch"
-    prof = os.path.join(ROOT, "profiles", "level_bf16_512.json")
+    prof = os.path.join(ROOT, "profiles", "level_l0w_f16_512_traffic.json")
     if os.path.exists(prof):
         with open(prof) as f:
             pj = json.load(f)
