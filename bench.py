@@ -721,7 +721,8 @@ def batch_bench(device, K, W):
             "achieved_tflops": flop / (ms_batch * 1e-3) / 1e12,
             "frac_of_peak": flop / (ms_batch * 1e-3) / 1e12 / peak_tf,
             "peak_source": f"{src} bf16 burst",
-            "autotuned": {"epilogue_unit": cfg.epilogue_unit, "stages": cfg.stages,
+            "autotuned": {"tiles_in_flight": cfg.tiles_in_flight,
+                          "epilogue_unit": cfg.epilogue_unit, "stages": cfg.stages,
                           "ctas": cfg.ctas, "best_ms": tuned_ms, "tuning_s": round(tune_s, 3)},
             "per_level_bf16_ms": ms_bf16, "per_level_fp32_ms": ms_fp32,
             "speedup_vs_fp32_per_model": ms_fp32 / ms_batch,

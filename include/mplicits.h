@@ -424,16 +424,23 @@ typedef struct {
 } MplBatchEntry;
 
 typedef struct {
-  void* workspace_dev; /* the device entry table */
+  void* workspace_dev; /* the device entry table (entries grouped by width) */
   int32_t count;
   int32_t precision;
+  int32_t width_count[3]; /* entries of padded width 64, 128, 256, in table order */
+  int32_t reserved;
 } MplBatchPlan;
 
 typedef struct {
-  int32_t epilogue_unit; /* 16 or 32 features per epilogue warp (0: 16)   */
-  int32_t stages;        /* weight-ring depth, 2 or 3 (0: 3)               */
-  int32_t ctas;          /* persistent CTAs (0: one per SM)                */
-  int32_t reserved;
+  int32_t epilogue_unit;   /* 16 or 32 features per epilogue warp (0: 32)   */
+  int32_t stages;          /* weight-ring depth of the one-tile pipeline,
+                              2 or 3 (0: 3); the two-tile pipeline takes the
+                              level kernel's ring per width (0 only)       */
+  int32_t ctas;            /* persistent CTAs (0: one per SM)              */
+  int32_t tiles_in_flight; /* 2: two tiles per CTA with first-layer warps,
+                              one launch per width present (unit 32 only);
+                              1: one tile, first layer in the epilogue
+                              warps, one launch (0: 2)                     */
 } MplBatchConfig;
 
 /* Bytes of the device workspace that holds a plan of `count` entries. */
@@ -448,8 +455,9 @@ int mpl_batch_prepare(const MplBatchEntry* entries, int32_t count, int32_t preci
 /* One persistent launch over every tile of every entry; no host sync, so it
  * can be captured in a CUDA graph.  config nullable (defaults). */
 int mpl_batch_run(const MplBatchPlan* plan, const MplBatchConfig* config, void* stream);
-/* Times every configuration (epilogue unit x weight-ring depth) on the plan
- * itself, `repeats` runs each after a warm-up run, and returns the fastest
+/* Times every configuration (tiles in flight x epilogue unit x weight-ring
+ * depth) on the plan itself, `repeats` runs each after a warm-up run, and
+ * returns the fastest
  * (minimum time) in *best and *best_ms.  Synchronises; the entries' outputs
  * afterwards hold the result of repeated runs (re-initialise S of
  * MPL_ACCUMULATE entries before the real run). */

@@ -2,8 +2,9 @@
 
 ``BatchedLevels`` takes a list of (level, points) entries, writes the device
 entry table once (``mpl_batch_prepare``), picks the kernel configuration with
-the library's autotuner (epilogue unit width x weight-ring depth, timed on
-the plan itself and cached per plan signature), and evaluates every entry in
+the library's autotuner (one or two tiles per CTA x epilogue unit width x
+weight-ring depth, timed on the plan itself and cached per plan signature),
+and evaluates every entry in
 ONE persistent launch (``mpl_batch_run``), optionally replayed from a CUDA
 graph.  It replaces the reference's one launch chain per model and level
 (renderer/cuda/gemms.cu:5-192, i3d/meshing.py:212-236).

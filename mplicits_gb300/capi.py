@@ -95,14 +95,16 @@ class MplBatchEntry(ctypes.Structure):
 class MplBatchPlan(ctypes.Structure):
     _fields_ = [("workspace_dev", ctypes.c_void_p),
                 ("count", ctypes.c_int32),
-                ("precision", ctypes.c_int32)]
+                ("precision", ctypes.c_int32),
+                ("width_count", ctypes.c_int32 * 3),
+                ("reserved", ctypes.c_int32)]
 
 
 class MplBatchConfig(ctypes.Structure):
     _fields_ = [("epilogue_unit", ctypes.c_int32),
                 ("stages", ctypes.c_int32),
                 ("ctas", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("tiles_in_flight", ctypes.c_int32)]
 
 
 MPL_BATCH_MAX_ENTRIES = 1024

@@ -75,7 +75,9 @@ struct Args {
   const Entry* entries;
   int32_t count;
   int* status;
+  int32_t* tiles;  // [count + 1] tile prefix in the workspace (two-tile kernel)
 };
+
 
 template <int STAGES, int U>
 struct Cfg {

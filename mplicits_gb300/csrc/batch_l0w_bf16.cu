@@ -1,0 +1,8 @@
+// Two-tile batched kernel instantiations, BF16 operands.
+#include "batch_launch.h"
+
+namespace mpl {
+namespace batch {
+int launch_p_u32_bf16(const Args& a, int WP, int c, cudaStream_t s) { return launch_l0w<32, 8, __nv_bfloat16>(a, WP, c, s); }
+}  // namespace batch
+}  // namespace mpl

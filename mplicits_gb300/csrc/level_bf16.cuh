@@ -186,17 +186,27 @@ __device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
   return d;
 }
 
+// Four consecutive weights of the first-layer image: from shared memory, or
+// (GW) through the read-only path of global memory.
+template <bool GW>
+__device__ __forceinline__ float4 w0_load4(const float* p) {
+  if (GW) return __ldg(reinterpret_cast<const float4*>(p));
+  return *reinterpret_cast<const float4*>(p);
+}
+
 // First-layer phases z_j = omega0 (W0 x + b0)_j of features j..j+3 for one
 // point, evaluated as fma(x, wx, fma(y, wy, fma(z, wz, wb))) two features at
-// a time.  w0s is the [4][stride] image (rows: omega0 W0[:, 0..2], omega0 b0);
-// the x, y, z weights are returned for the tangent rows.
+// a time.  w0s is the [4][stride] image (rows: omega0 W0[:, 0..2], omega0 b0)
+// in shared memory, or in global memory when GW; the x, y, z weights are
+// returned for the tangent rows.
+template <bool GW = false>
 __device__ __forceinline__ void phase4(const float* w0s, int stride, int j, float x, float y,
                                        float z, float (&zz)[4], float4& wx, float4& wy,
                                        float4& wz) {
-  wx = *reinterpret_cast<const float4*>(w0s + j);
-  wy = *reinterpret_cast<const float4*>(w0s + stride + j);
-  wz = *reinterpret_cast<const float4*>(w0s + 2 * stride + j);
-  const float4 wb = *reinterpret_cast<const float4*>(w0s + 3 * stride + j);
+  wx = w0_load4<GW>(w0s + j);
+  wy = w0_load4<GW>(w0s + stride + j);
+  wz = w0_load4<GW>(w0s + 2 * stride + j);
+  const float4 wb = w0_load4<GW>(w0s + 3 * stride + j);
   const uint64_t X = f2pack(x, x), Y = f2pack(y, y), Z = f2pack(z, z);
   const uint64_t a = ffma2(X, f2pack(wx.x, wx.y),
                            ffma2(Y, f2pack(wy.x, wy.y), ffma2(Z, f2pack(wz.x, wz.y),
@@ -211,7 +221,8 @@ __device__ __forceinline__ void phase4(const float* w0s, int stride, int j, floa
 // Layer 0 of one U-feature unit (features j0..j0+U-1) for this thread's row:
 // FP32 phase omega0*(W0 x + b0) (omega folded into w0s), sine, 16-bit into
 // the A operand.  GRAD: tangent row ch gets cos(z) * omega0*W0[:, ch-1].
-template <typename T, bool GRAD, int U>
+// GW: w0s lives in global memory.
+template <typename T, bool GRAD, int U, bool GW = false>
 __device__ __forceinline__ void layer0_unit(uint8_t* sA, const float* w0s, int stride, int m,
                                             int j0, int ch, float phase, float x, float y,
                                             float z) {
@@ -220,7 +231,7 @@ __device__ __forceinline__ void layer0_unit(uint8_t* sA, const float* w0s, int s
   for (int j4 = 0; j4 < U / 4; ++j4) {
     float zz[4];
     float4 wx, wy, wz;
-    phase4(w0s, stride, j0 + 4 * j4, x, y, z, zz, wx, wy, wz);
+    phase4<GW>(w0s, stride, j0 + 4 * j4, x, y, z, zz, wx, wy, wz);
     const float ax[4] = {wx.x, wx.y, wx.z, wx.w};
     const float ay[4] = {wy.x, wy.y, wy.z, wy.w};
     const float az[4] = {wz.x, wz.y, wz.z, wz.w};

@@ -67,19 +67,20 @@ def _single(entries, precision):
     return outs
 
 
-@pytest.mark.parametrize("precision", ["bf16", "fp16"])
-@pytest.mark.parametrize("unit,stages", [(16, 3), (16, 2), (32, 3), (32, 2)])
-def test_batched_launch_equals_single_level_launches(lib, precision, unit, stages):
+CONFIGS = [(1, 16, 3), (1, 16, 2), (1, 32, 3), (1, 32, 2), (2, 32, 0)]
+
+
+def _check_against_single(entries, precision, tiles, unit, stages, ctas=0):
     from mplicits_gb300 import capi
     from mplicits_gb300.batch import BatchedLevels
-    entries, _ = _entries(precision)
     init = [e.S.clone() for e in entries]
     old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
     capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, unit)
     try:
         ref = _single(entries, precision)
         bl = BatchedLevels(entries, precision)
-        bl.run(capi.MplBatchConfig(epilogue_unit=unit, stages=stages))
+        bl.run(capi.MplBatchConfig(epilogue_unit=unit, stages=stages, ctas=ctas,
+                                   tiles_in_flight=tiles))
         torch.cuda.synchronize()
     finally:
         capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
@@ -88,6 +89,60 @@ def test_batched_launch_equals_single_level_launches(lib, precision, unit, stage
         assert torch.equal(e.S, r), i
         if e.n > 50:
             assert not torch.equal(e.S, init[i]), i
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
+@pytest.mark.parametrize("tiles,unit,stages", CONFIGS)
+def test_batched_launch_equals_single_level_launches(lib, precision, tiles, unit, stages):
+    entries, _ = _entries(precision)
+    _check_against_single(entries, precision, tiles, unit, stages)
+
+
+@pytest.mark.parametrize("tiles,unit,stages,ctas", [(2, 32, 0, 0), (2, 32, 0, 7), (1, 32, 3, 5),
+                                                    (1, 16, 2, 0)])
+def test_many_small_entries_of_mixed_shapes(lib, tiles, unit, stages, ctas):
+    """Hundreds of entries of one to a few tiles each, widths and depths
+    mixed, so that nearly every tile of a CTA changes entry (the slots'
+    constants are refilled over and over) and rounds end with one slot
+    empty; also a grid smaller than the two slots of one round."""
+    from mplicits_gb300.batch import BatchEntry
+    rng = np.random.default_rng(11)
+    g = torch.Generator("cuda").manual_seed(11)
+    models = {}
+    for w in (64, 128, 256):
+        for d in (2, 3):
+            models[(w, d)] = _model(w, d, 7 * w + d, "bf16")
+    entries = []
+    for i in range(300):
+        w = int(rng.choice([64, 128, 256]))
+        d = int(rng.choice([2, 3]))
+        n = int(rng.integers(0, 400))
+        P = n + 3
+        x = torch.rand(P, 3, device="cuda", generator=g) * 2 - 1
+        kw = {}
+        if i % 7 == 3:
+            kw["index"] = torch.from_numpy(rng.permutation(P)[:n].astype(np.int32)).cuda()
+        entries.append(BatchEntry(models[(w, d)], torch.full((P,), 5.0, device="cuda"), x=x,
+                                  n=n, accumulate=(i % 11 == 5), **kw))
+    _check_against_single(entries, "bf16", tiles, unit, stages, ctas)
+
+
+def test_two_tile_pipeline_rejects_a_ring_depth_and_16_wide_units(lib):
+    import ctypes
+    from mplicits_gb300 import capi
+    from mplicits_gb300.batch import BatchedLevels
+    entries, _ = _entries("bf16")
+    bl = BatchedLevels(entries[:2], "bf16")
+    assert list(bl.plan.width_count) == [0, 1, 1]  # widths 256 and 128, grouped
+    cfg = capi.MplBatchConfig(epilogue_unit=32, stages=2, tiles_in_flight=2)
+    assert capi.load().mpl_batch_run(ctypes.byref(bl.plan), ctypes.byref(cfg),
+                                     capi.stream_ptr()) == capi.MPL_ERR_UNSUPPORTED
+    cfg = capi.MplBatchConfig(epilogue_unit=16, tiles_in_flight=2)
+    assert capi.load().mpl_batch_run(ctypes.byref(bl.plan), ctypes.byref(cfg),
+                                     capi.stream_ptr()) == capi.MPL_ERR_UNSUPPORTED
+    cfg = capi.MplBatchConfig(tiles_in_flight=3)
+    assert capi.load().mpl_batch_run(ctypes.byref(bl.plan), ctypes.byref(cfg),
+                                     capi.stream_ptr()) == capi.MPL_ERR_INVALID_ARG
 
 
 def test_batched_launch_within_bf16_error_of_fp32(lib):
@@ -116,7 +171,8 @@ def test_autotune_and_graph_replay(lib):
         e.accumulate = False
     bl = BatchedLevels(entries, "bf16")
     cfg, ms = bl.autotune(repeats=2)
-    assert cfg.epilogue_unit in (16, 32) and cfg.stages in (2, 3) and ms > 0
+    assert cfg.epilogue_unit in (16, 32) and cfg.stages in (0, 2, 3) and ms > 0
+    assert cfg.tiles_in_flight in (1, 2)
     for e in entries:
         e.S.fill_(-3.0)
     old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
@@ -132,7 +188,8 @@ def test_autotune_and_graph_replay(lib):
         assert torch.equal(e.S, r)
     # the cache answers the same signature without timing again
     cfg2, ms2 = BatchedLevels(entries, "bf16").autotune()
-    assert (cfg2.epilogue_unit, cfg2.stages, ms2) == (cfg.epilogue_unit, cfg.stages, ms)
+    assert (cfg2.tiles_in_flight, cfg2.epilogue_unit, cfg2.stages, ms2) == \
+        (cfg.tiles_in_flight, cfg.epilogue_unit, cfg.stages, ms)
 
 
 def test_batch_rejects_unsupported_entries(lib):
