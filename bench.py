@@ -727,7 +727,10 @@ def batch_bench(device, K, W):
             "per_level_bf16_ms": ms_bf16, "per_level_fp32_ms": ms_fp32,
             "speedup_vs_fp32_per_model": ms_fp32 / ms_batch,
             "speedup_vs_bf16_per_level": ms_bf16 / ms_batch,
-            "gpu_launches_per_step": 1}
+            # two tiles in flight: a tile-prefix kernel and the batched kernel
+            # per width group present; one tile: one launch
+            "gpu_launches_per_step": (2 * sum(1 for c in bl.plan.width_count if c > 0)
+                                      if cfg.tiles_in_flight == 2 else 1)}
 
 
 def run_reference(args):
