@@ -39,9 +39,9 @@ __device__ __forceinline__ int64_t level_point_count(const LevelArgs& a) {
   return n < 0 ? 0 : n;
 }
 
-__device__ __forceinline__ void load_point(const LevelArgs& a, int64_t q, int64_t& p, float& x,
-                                           float& y, float& z) {
-  p = a.index ? (int64_t)a.index[q] : q;
+// Coordinates of point p (grid index or row of the point list).
+__device__ __forceinline__ void point_coords(const LevelArgs& a, int64_t p, float& x, float& y,
+                                             float& z) {
   if (a.pts.kind == MPL_POINTS_GRID) {
     grid_point(p, a.pts.grid_n, a.pts.voxel_size, a.pts.offset[0], a.pts.offset[1],
                a.pts.offset[2], x, y, z);
@@ -50,6 +50,12 @@ __device__ __forceinline__ void load_point(const LevelArgs& a, int64_t q, int64_
     y = a.pts.xyz[3 * p + 1];
     z = a.pts.xyz[3 * p + 2];
   }
+}
+
+__device__ __forceinline__ void load_point(const LevelArgs& a, int64_t q, int64_t& p, float& x,
+                                           float& y, float& z) {
+  p = a.index ? (int64_t)a.index[q] : q;
+  point_coords(a, p, x, y, z);
 }
 
 // Stores f into S[p] (or adds it) and appends p to the band list when

@@ -262,33 +262,42 @@ __global__ void __launch_bounds__(Roles<U, NL>::kThreads, 1) level_l0w_kernel(co
     const int ch = GRAD ? (m & 3) : 0;
     const float phase = ch ? 1.57079632679489662f : 0.f;
     const int prow = GRAD ? (m >> 2) : m;
+    // The warp's tiles in order k = 2 r + s (tile blockIdx.x + k gridDim.x);
+    // a row's point id is read one tile ahead, so that the gather from an
+    // index list (band lists) lands while the previous tile is computed.
+    auto point_id = [&](int64_t t) -> int64_t {
+      const int64_t qi = t * PT + prow;
+      return qi < n ? (a.index ? (int64_t)a.index[qi] : qi) : -1;
+    };
+    const int64_t nt = (ntiles - blockIdx.x + G - 1) / G;
+    int64_t pn = point_id(blockIdx.x);
     bool ok = true;
-    for (int64_t r = 0; r < nrounds && ok; ++r) {
-      for (int s = 0; s < 2 && ok; ++s) {
-        const int64_t t = tile_of(r, s);
-        if (t >= ntiles) continue;
-        float x = 0.f, y = 0.f, z = 0.f;
-        const int64_t qi = t * PT + prow;
-        int64_t pq = -1;
-        if (qi < n) load_point(a, qi, pq, x, y, z);
-        // the slot's previous tile has finished its last GEMM (the reader of
-        // the A operand written here)
-        if (r > 0 &&
-            !bf16::warp_wait(&afree[s], (uint32_t)((r - 1) & 1), a.status, abort_flag)) {
-          ok = false;
-          break;
-        }
-        uint8_t* sA = smem + C::oA + s * C::kABytes;
 #pragma unroll 1
-        for (int c = 0; c < NC; ++c) {
+    for (int64_t k = 0; k < nt && ok; ++k) {
+      const int64_t t = (int64_t)blockIdx.x + k * G;
+      const int64_t r = k >> 1;
+      const int s = (int)(k & 1);
+      const int64_t p = pn;
+      if (k + 1 < nt) pn = point_id(t + G);
+      float x = 0.f, y = 0.f, z = 0.f;
+      if (p >= 0) point_coords(a, p, x, y, z);
+      // the slot's previous tile has finished its last GEMM (the reader of
+      // the A operand written here)
+      if (r > 0 &&
+          !bf16::warp_wait(&afree[s], (uint32_t)((r - 1) & 1), a.status, abort_flag)) {
+        ok = false;
+        break;
+      }
+      uint8_t* sA = smem + C::oA + s * C::kABytes;
+#pragma unroll 1
+      for (int c = 0; c < NC; ++c) {
 #pragma unroll
-          for (int u = 0; u < kF / 16; ++u)
-            bf16::layer0_unit<T, GRAD, 16>(sA, w0s, WP, m, c * kKC + f0 + u * 16, ch, phase, x,
-                                            y, z);
-          fence_proxy_async_smem();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&l0chunk[s * kMaxNC + c]);
-        }
+        for (int u = 0; u < kF / 16; ++u)
+          bf16::layer0_unit<T, GRAD, 16>(sA, w0s, WP, m, c * kKC + f0 + u * 16, ch, phase, x,
+                                          y, z);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&l0chunk[s * kMaxNC + c]);
       }
     }
   } else {
