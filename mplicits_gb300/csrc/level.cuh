@@ -62,6 +62,32 @@ __device__ __forceinline__ void load_point(const LevelArgs& a, int64_t q, int64_
 // |S[p]| < delta.  Called by every lane of a full warp; `valid` masks lanes
 // without a point.
 __device__ __forceinline__ void store_and_band(const LevelArgs& a, bool valid, int64_t p,
+                                               float f);
+
+// As store_and_band, with the value S[p] held before this level already read
+// (MPL_ACCUMULATE; ignored in MPL_STORE), so that its load can be issued early.
+__device__ __forceinline__ void store_and_band_old(const LevelArgs& a, bool valid, int64_t p,
+                                                   float f, float old) {
+  float s = f;
+  if (valid) {
+    if (a.store_mode == MPL_ACCUMULATE) s = __fadd_rn(old, f);
+    a.S[p] = s;
+  }
+  if (a.has_band) {
+    const bool keep = valid && fabsf(s) < a.band_delta && fabsf(s) >= a.band_lower;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(a.band_count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) {
+      const int64_t pos = (int64_t)base + __popc(m & ((1u << lane) - 1u));
+      if (pos < a.band_capacity) a.band_out[pos] = (int32_t)p;
+    }
+  }
+}
+
+__device__ __forceinline__ void store_and_band(const LevelArgs& a, bool valid, int64_t p,
                                                float f) {
   float s = f;
   if (valid) {

@@ -375,6 +375,10 @@ __global__ void __launch_bounds__(Roles<U, NL>::kThreads, 1) level_l0w_kernel(co
               }
             }
           }
+          // the value this level adds to, read while the reduction below waits
+          // (the point id has arrived during the drain)
+          float sold = 0.f;
+          if (!GRAD && ps >= 0 && a.store_mode == MPL_ACCUMULATE) sold = a.S[ps];
           // the slot's next GEMM waits for the whole drain (it overwrites the
           // accumulator), so the A chunks written here are handed over at once
           if (l < nh) fence_proxy_async_smem();
@@ -416,7 +420,7 @@ __global__ void __launch_bounds__(Roles<U, NL>::kThreads, 1) level_l0w_kernel(co
               }
               store_and_band(a, ps >= 0 && ch == 0, ps, __fadd_rn(sum, bout));
             } else {
-              store_and_band(a, ps >= 0, ps, __fadd_rn(sum, bout));
+              store_and_band_old(a, ps >= 0, ps, __fadd_rn(sum, bout), sold);
             }
           }
         }
