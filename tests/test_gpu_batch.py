@@ -98,9 +98,10 @@ def test_batched_launch_equals_single_level_launches(lib, precision, tiles, unit
     _check_against_single(entries, precision, tiles, unit, stages)
 
 
-@pytest.mark.parametrize("tiles,unit,stages,ctas", [(2, 32, 0, 0), (2, 32, 0, 7), (1, 32, 3, 5),
-                                                    (1, 16, 2, 0)])
-def test_many_small_entries_of_mixed_shapes(lib, tiles, unit, stages, ctas):
+@pytest.mark.parametrize("tiles,unit,stages,ctas,precision",
+                         [(2, 32, 0, 0, "bf16"), (2, 32, 0, 7, "bf16"), (2, 32, 0, 0, "fp16"),
+                          (1, 32, 3, 5, "bf16"), (1, 16, 2, 0, "bf16")])
+def test_many_small_entries_of_mixed_shapes(lib, tiles, unit, stages, ctas, precision):
     """Hundreds of entries of one to a few tiles each, widths and depths
     mixed, so that nearly every tile of a CTA changes entry (the slots'
     constants are refilled over and over) and rounds end with one slot
@@ -111,7 +112,7 @@ def test_many_small_entries_of_mixed_shapes(lib, tiles, unit, stages, ctas):
     models = {}
     for w in (64, 128, 256):
         for d in (2, 3):
-            models[(w, d)] = _model(w, d, 7 * w + d, "bf16")
+            models[(w, d)] = _model(w, d, 7 * w + d, precision)
     entries = []
     for i in range(300):
         w = int(rng.choice([64, 128, 256]))
@@ -124,7 +125,7 @@ def test_many_small_entries_of_mixed_shapes(lib, tiles, unit, stages, ctas):
             kw["index"] = torch.from_numpy(rng.permutation(P)[:n].astype(np.int32)).cuda()
         entries.append(BatchEntry(models[(w, d)], torch.full((P,), 5.0, device="cuda"), x=x,
                                   n=n, accumulate=(i % 11 == 5), **kw))
-    _check_against_single(entries, "bf16", tiles, unit, stages, ctas)
+    _check_against_single(entries, precision, tiles, unit, stages, ctas)
 
 
 def test_two_tile_pipeline_rejects_a_ring_depth_and_16_wide_units(lib):
@@ -190,6 +191,39 @@ def test_autotune_and_graph_replay(lib):
     cfg2, ms2 = BatchedLevels(entries, "bf16").autotune()
     assert (cfg2.tiles_in_flight, cfg2.epilogue_unit, cfg2.stages, ms2) == \
         (cfg.tiles_in_flight, cfg.epilogue_unit, cfg.stages, ms)
+
+
+def test_graph_replay_follows_device_counts(lib):
+    """Device counts changed between replays of one captured graph: the
+    tile prefix is rebuilt on the device by every replay."""
+    from mplicits_gb300 import capi
+    from mplicits_gb300.batch import BatchEntry, BatchedLevels
+    g = torch.Generator("cuda").manual_seed(21)
+    entries, counts = [], []
+    for i, (w, d, P) in enumerate([(256, 3, 3000), (128, 3, 5000), (256, 2, 700), (128, 2, 900)]):
+        m = _model(w, d, 300 + i, "bf16")
+        x = torch.rand(P, 3, device="cuda", generator=g) * 2 - 1
+        c = torch.tensor([P], dtype=torch.int32, device="cuda")
+        counts.append(c)
+        entries.append(BatchEntry(m, torch.zeros(P, device="cuda"), x=x, n=P, n_dev=c))
+    bl = BatchedLevels(entries, "bf16")
+    bl.config = capi.MplBatchConfig(epilogue_unit=32, tiles_in_flight=2)
+    bl.capture()
+    old = capi.get_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT)
+    capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, 32)
+    try:
+        for frac in (1.0, 0.37, 0.0, 0.81):
+            for e, c in zip(entries, counts):
+                c.fill_(int(e.n * frac))
+                e.S.fill_(9.0)
+            ref = _single(entries, "bf16")
+            bl.replay()
+            torch.cuda.synchronize()
+            for i, (e, r) in enumerate(zip(entries, ref)):
+                assert torch.equal(e.S, r), (frac, i)
+    finally:
+        capi.set_option(capi.MPL_OPT_BF16_EPILOGUE_UNIT, old)
+    assert capi.device_status() == capi.MPL_OK
 
 
 def test_batch_rejects_unsupported_entries(lib):
