@@ -452,13 +452,15 @@ int mpl_batch_workspace_bytes(int32_t count, int64_t* bytes);
 int mpl_batch_prepare(const MplBatchEntry* entries, int32_t count, int32_t precision,
                       void* workspace_dev, int64_t workspace_bytes, MplBatchPlan* plan,
                       void* stream);
-/* One persistent launch over every tile of every entry; no host sync, so it
- * can be captured in a CUDA graph.  config nullable (defaults). */
+/* The plan's tiles in persistent launches: with two tiles in flight (the
+ * default) a tile-prefix kernel and one batched kernel per width group
+ * present, in stream order; with one tile, one launch over every entry.  No
+ * host sync, so it can be captured in a CUDA graph (device counts are read by
+ * every replay).  config nullable (defaults). */
 int mpl_batch_run(const MplBatchPlan* plan, const MplBatchConfig* config, void* stream);
 /* Times every configuration (tiles in flight x epilogue unit x weight-ring
  * depth) on the plan itself, `repeats` runs each after a warm-up run, and
- * returns the fastest
- * (minimum time) in *best and *best_ms.  Synchronises; the entries' outputs
+ * returns the fastest (minimum time) in *best and *best_ms.  Synchronises; the entries' outputs
  * afterwards hold the result of repeated runs (re-initialise S of
  * MPL_ACCUMULATE entries before the real run). */
 int mpl_batch_autotune(const MplBatchPlan* plan, int32_t repeats, MplBatchConfig* best,
