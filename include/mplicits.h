@@ -403,7 +403,8 @@ int mpl_calc_deltas(const MplScene* scene, const float* vertices_dev, int64_t n_
 /* No single reference entry point: this replaces the reference's one launch
  * chain per model and per level (renderer/cuda/gemms.cu:5-192 NeuralImplicit,
  * and the per-level loop of i3d/meshing.py:212-236) by one persistent launch
- * over all entries.  Entries are levels with 1 or 2 hidden GEMMs of width
+ * per width group of entries (see mpl_batch_run).  Entries are levels with 1
+ * or 2 hidden GEMMs of width
  * <= 256 (padded widths 64/128/256 may mix); each runs on its own point list
  * (points + optional index list, count optionally on the device) and stores
  * or accumulates into its own S.  Tensor-core operands only (MPL_BF16 or
