@@ -1,12 +1,12 @@
-"""Serving-style evaluation of many levels of many models in one launch.
+"""Serving-style evaluation of many levels of many models in persistent
+launches.
 
 ``BatchedLevels`` takes a list of (level, points) entries, writes the device
-entry table once (``mpl_batch_prepare``), picks the kernel configuration with
-the library's autotuner (one or two tiles per CTA x epilogue unit width x
-weight-ring depth, timed on the plan itself and cached per plan signature),
-and evaluates every entry in
-ONE persistent launch (``mpl_batch_run``), optionally replayed from a CUDA
-graph.  It replaces the reference's one launch chain per model and level
+entry table once (``mpl_batch_prepare``, entries grouped by width), picks the
+kernel configuration with the library's autotuner (one or two tiles per CTA x
+epilogue unit width x weight-ring depth, timed on the plan itself and cached
+per plan signature), and evaluates every entry in one persistent launch per
+width group (``mpl_batch_run``), optionally replayed from a CUDA graph.  It replaces the reference's one launch chain per model and level
 (renderer/cuda/gemms.cu:5-192, i3d/meshing.py:212-236).
 
 Entries write disjoint outputs: tiles of different entries run concurrently,
