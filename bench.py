@@ -7,11 +7,13 @@ synthetic surface r = 0.6 + 0.03 sin(12 theta) sin(12 phi)
 gen_mc_coordinate_grid; bands delta0 = 0.05, delta1 = 0.01; marching cubes at
 0.  One step = level 0 on all 134,217,728 grid points (fused band list),
 level 1 on band 1, level 2 on band 2, marching cubes (count + emit) on the
-device.  ``value`` is grid points per second of that step with the BF16
-tcgen05 kernels; the same step with the plain FP32 kernels, the error of both
+device.  ``value`` is grid points per second of that step with the 16-bit
+tcgen05 kernels (FP16 operands, the form that meets the SDF error target;
+BF16 beside it); the same step with the plain FP32 kernels, the error of each
 against the FP64 oracle, the end-to-end number through the public API with
 host buffers, the CPU baseline and the roofline of the dominant kernel are in
-the same JSON line.
+the same JSON line, next to the training step, sphere tracing, the batched
+64-model launch and calc_deltas sub-benchmarks.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
